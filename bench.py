@@ -1,0 +1,374 @@
+"""Benchmark of the fused LBM stream–collide step on GB300.
+
+Default workload: D3Q19 SRT lid-driven cube 256^3, float32 storage and arithmetic, Re = 100,
+lid u = 0.1 (tau = 3*0.1*255/100 + 0.5 = 1.265), two-lattice pull streaming (double buffer),
+six bounce-back walls with a moving lid — the D3Q19 configuration the headline metric (D3Q19
+MLUPs, % HBM roofline) is quoted on.  A step is one lattice update of every cell.
+
+  python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference] [--workload NAME]
+
+One JSON line on rank 0.  `value` = MLUPs of all ranks with the lattices already resident in
+HBM (2 x 1.27 GB, larger than the 129 MB L2, so no flush is needed between steps); `e2e` = the
+same job through the public API (Solver.run) from pinned host buffers, the upload of f/bc/flags
+and the download of f inside the timed region.  Multi-GPU runs are independent replicas (the
+step has no exchange on one domain per GPU): value = cells x steps of all ranks / max time.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import math
+import os
+import re
+import statistics
+import subprocess
+import sys
+import time
+from pathlib import Path
+
+import numpy as np
+
+ROOT = Path(__file__).resolve().parent
+sys.path.insert(0, str(ROOT))
+
+BYTES_PER_UPDATE = {("D2Q9", False): 72, ("D3Q19", False): 152, ("D3Q19", True): 76, ("D3Q27", False): 216,
+                    ("D3Q27", True): 108}
+
+WORKLOADS = {
+    # name: (lattice, n, method, collision, LES, float16c+DDF, Re, lid u, tile)
+    "ldc3d_d3q19_256_fp32": dict(lattice="D3Q19", n=256, method="db", coll="SRT", les=False, f16=False, Re=100.0,
+                                 U=0.1, tile=(8, 8, 4),
+                                 desc="D3Q19 SRT lid-driven cube 256^3, FP32/FP32, Re=100, lid u=0.1, "
+                                      "two-lattice pull streaming (double buffer)"),
+    "ldc3d_d3q19_256_f16c": dict(lattice="D3Q19", n=256, method="db", coll="SRT", les=False, f16=True, Re=100.0,
+                                 U=0.1, tile=(8, 8, 4),
+                                 desc="D3Q19 SRT lid-driven cube 256^3, Float16C storage + DDF shift, FP32 math, "
+                                      "Re=100, lid u=0.1, pull streaming"),
+    "ldc3d_d3q27_256_kbc_f16c_eso": dict(lattice="D3Q27", n=256, method="eso", coll="KBC", les=True, f16=True,
+                                         Re=10000.0, U=0.1, tile=(8, 8, 4),
+                                         desc="D3Q27 KBC + Smagorinsky Cs=0.1 lid-driven cube 256^3, Re=10000, "
+                                              "Float16C + DDF shift, FP32 math, esoteric-pull in place"),
+}
+DEFAULT_WORKLOAD = "ldc3d_d3q19_256_fp32"
+
+
+# ---------------------------------------------------------------------------------------------
+def dist_env():
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return rank, world, local
+
+
+def aggregate(local_ms: float, local_units: float, world: int, backend_device=None):
+    """Max of the per-rank times and sum of the per-rank units (replicas).  With world == 1 no
+    process group is needed."""
+    if world == 1:
+        return local_ms, local_units
+    import torch
+    import torch.distributed as dist
+    t = torch.tensor([local_ms, -local_units], dtype=torch.float64, device=backend_device)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    u = torch.tensor([local_units], dtype=torch.float64, device=backend_device)
+    dist.all_reduce(u, op=dist.ReduceOp.SUM)
+    return float(t[0]), float(u[0])
+
+
+def barrier(world: int):
+    if world > 1:
+        import torch.distributed as dist
+        dist.barrier()
+
+
+def measured_peaks():
+    p = ROOT / "MEASURED_PEAKS.json"
+    if p.exists():
+        d = json.loads(p.read_text())
+        return float(d["hbm_gbs"]), "measured"
+    return 6800.0, "fallback"
+
+
+def profiled_traffic(workload: str):
+    """DRAM bytes per launch of the step kernel from the committed ncu summary, if present."""
+    p = ROOT / "profiles" / f"{workload}.txt"
+    if not p.exists():
+        return None, None
+    m = re.search(r"^dram_bytes_per_launch_full:\s*([0-9.eE+]+)", p.read_text(), re.M)
+    return (float(m.group(1)) if m else None), str(p.relative_to(ROOT))
+
+
+class ClockSampler:
+    """Samples nvidia-smi clocks and throttle reasons while running (200 ms period)."""
+    QUERY = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,clocks_event_reasons.hw_slowdown,"
+             "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+             "clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu_index: int):
+        self.proc = None
+        self.out = None
+        try:
+            self.out = open(os.devnull if not os.access(".", os.W_OK) else "/tmp/_lbm_clocks.csv", "w")
+            self.proc = subprocess.Popen(["nvidia-smi", f"--id={gpu_index}", f"--query-gpu={self.QUERY}",
+                                          "--format=csv,noheader,nounits", "-lms", "200"], stdout=self.out,
+                                         stderr=subprocess.DEVNULL)
+        except Exception:
+            self.proc = None
+
+    def stop(self):
+        if self.proc is None:
+            return None
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except Exception:
+            self.proc.kill()
+        self.out.close()
+        rows = []
+        for ln in Path("/tmp/_lbm_clocks.csv").read_text().splitlines():
+            parts = [p.strip() for p in ln.split(",")]
+            if len(parts) < 9:
+                continue
+            try:
+                rows.append((float(parts[1]), float(parts[2]), parts[5:9]))
+            except ValueError:
+                continue
+        if not rows:
+            return None
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = sorted({names[i] for _, _, r in rows for i, v in enumerate(r) if v.lower() == "active"})
+        return {"sm_mhz": statistics.median(r[0] for r in rows), "sm_max_mhz": max(r[1] for r in rows),
+                "reasons": reasons, "samples": len(rows)}
+
+
+# ---------------------------------------------------------------------------------------------
+def build_case(wl: dict):
+    """Grid, config, host flags/bc and tau of a workload (host numpy, tiled layout)."""
+    from mojo_lbm_gb300 import Flags, LBM_Config, LBM_Grid, LBM_method, preprocess
+    from mojo_lbm_gb300.lattice import get_lattice
+    lat_id = {"D2Q9": 0, "D3Q19": 1, "D3Q27": 2}[wl["lattice"]]
+    n = wl["n"]
+    grid = LBM_Grid(get_lattice(lat_id), n, n, n, wl["tile"])
+    method = LBM_method.DOUBLE_BUFFER if wl["method"] == "db" else LBM_method.ESOTERIC_PULL
+    cfg = LBM_Config(method, collision_op=wl["coll"], LES=wl["les"], DDF_shift=wl["f16"], use_float16c=wl["f16"])
+    N, D = grid.num_points, grid.D
+    flags = np.zeros(N, np.uint8)
+    bc = np.zeros(N * (D + 1), np.float32)
+    for s in ("-Y", "+X", "-X", "+Z", "-Z"):
+        preprocess.set_exterior_walls(grid, cfg, flags, bc, s, Flags.SOLID, [0.0] * D, 1.0)
+    preprocess.set_exterior_walls(grid, cfg, flags, bc, "+Y", Flags.SOLID, [wl["U"], 0.0, 0.0], 1.0)
+    tau = 3.0 * wl["U"] * (n - 1) / wl["Re"] + 0.5
+    return grid, cfg, flags, bc, tau
+
+
+def cpu_sample(wl: dict, grid, cfg, flags, bc, tau, budget_s: float, max_steps: int | None = None):
+    """Times the float32 CPU oracle (OpenMP over all host threads) on slabs of the same workload.
+    Returns (MLUPs, cores, description)."""
+    import oracle
+    N, Q = grid.num_points, grid.Q
+    f = np.zeros(N * Q, oracle.f_dtype(cfg, 32))
+    oracle.init(cfg, grid, 32, f)
+    f2 = f.copy() if wl["method"] == "db" else f
+    cores = oracle.max_threads()
+    slab = max(1, N // 16)
+    done_cells, t_total, k = 0, 0.0, 0
+    while (t_total < budget_s or k < 2) and (max_steps is None or k < max_steps):
+        b = (k * slab) % N
+        t0 = time.perf_counter()
+        oracle.step_range(cfg, grid, 32, f2, f, bc, flags, tau, k % 2 == 0, b, min(N, b + slab), cores)
+        t_total += time.perf_counter() - t0
+        done_cells += min(N, b + slab) - b
+        k += 1
+    return done_cells / t_total / 1e6, cores, f"{k} slab-steps of {slab} cells (1/16 of the grid) each, {t_total:.1f} s"
+
+
+# ---------------------------------------------------------------------------------------------
+def run_ours(args, wl: dict):
+    import torch
+    from mojo_lbm_gb300.solver import Solver
+
+    rank, world, local = dist_env()
+    if world > 1:
+        import torch.distributed as dist
+        torch.cuda.set_device(local)
+        dist.init_process_group("nccl")
+    dev = torch.device("cuda", local if world > 1 else 0)
+    torch.cuda.set_device(dev)
+
+    grid, cfg, flags, bc, tau = build_case(wl)
+    N, Q = grid.num_points, grid.Q
+    solver = Solver(grid, cfg)
+    if args.threads:
+        solver.set_block_threads(args.threads)
+    f_dtype = torch.int16 if cfg.use_float16c else torch.float32
+    fa = torch.empty(N * Q, dtype=f_dtype, device=dev)
+    fb = torch.empty_like(fa) if wl["method"] == "db" else fa
+    bct = torch.from_numpy(bc).to(dev)
+    flt = torch.from_numpy(flags).to(dev)
+    solver.init_equilibrium(fa)
+    if wl["method"] == "db":
+        fb.copy_(fa)
+    stream = torch.cuda.current_stream(dev)
+
+    # warm-up: W steps, then one graph replay so the 64-step graph is captured before timing
+    solver.run(fa, fb, bct, flt, tau, args.warmup, 0, stream)
+    solver.run(fa, fb, bct, flt, tau, 64, 0, stream)
+    torch.cuda.synchronize(dev)
+
+    # per-launch kernel duration with CUDA events on the launching stream
+    ev = [torch.cuda.Event(enable_timing=True) for _ in range(2 * 8)]
+    for i in range(8):
+        ev[2 * i].record(stream)
+        if wl["method"] == "db":
+            if i % 2 == 0:
+                solver.double_buffer_step(fb, fa, bct, flt, tau, stream)
+            else:
+                solver.double_buffer_step(fa, fb, bct, flt, tau, stream)
+        else:
+            solver.esoteric_pull_step(fa, bct, flt, tau, i % 2 == 0, stream)
+        ev[2 * i + 1].record(stream)
+    torch.cuda.synchronize(dev)
+    launch_ms = statistics.median(ev[2 * i].elapsed_time(ev[2 * i + 1]) for i in range(8))
+
+    # timed region: K steps from the graph, barrier + synchronize on both sides
+    clocks = ClockSampler(local) if rank == 0 else None
+    K = args.steps
+    barrier(world)
+    torch.cuda.synchronize(dev)
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    solver.run(fa, fb, bct, flt, tau, K, 0, stream)
+    e1.record(stream)
+    torch.cuda.synchronize(dev)
+    barrier(world)
+    local_ms = e0.elapsed_time(e1)
+    clk = clocks.stop() if clocks else None
+    t_ms, units = aggregate(local_ms, float(N) * K, world, dev)
+    mlups = units / (t_ms * 1e-3) / 1e6
+
+    # end to end through the public API from pinned host buffers
+    f_host = torch.empty(N * Q, dtype=f_dtype).pin_memory()
+    f_host.copy_(fa)
+    bc_host = torch.from_numpy(bc).pin_memory()
+    fl_host = torch.from_numpy(flags).pin_memory()
+    out_host = torch.empty_like(f_host).pin_memory()
+    barrier(world)
+    torch.cuda.synchronize(dev)
+    h0, h1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    h0.record(stream)
+    fa.copy_(f_host, non_blocking=True)
+    bct.copy_(bc_host, non_blocking=True)
+    flt.copy_(fl_host, non_blocking=True)
+    if wl["method"] == "db":
+        fb.copy_(fa)
+    solver.run(fa, fb, bct, flt, tau, K, 0, stream)
+    out_host.copy_(fa if (K % 2 == 0 or wl["method"] != "db") else fb, non_blocking=True)
+    h1.record(stream)
+    torch.cuda.synchronize(dev)
+    barrier(world)
+    e2e_ms, e2e_units = aggregate(h0.elapsed_time(h1), float(N) * K, world, dev)
+    e2e_mlups = e2e_units / (e2e_ms * 1e-3) / 1e6
+    h2d = f_host.numel() * f_host.element_size() + bc_host.numel() * 4 + fl_host.numel()
+    d2h = out_host.numel() * out_host.element_size()
+
+    if rank != 0:
+        return None
+    key = (wl["lattice"], wl["f16"])
+    b_alg = BYTES_PER_UPDATE[key]
+    achieved = b_alg * N / (launch_ms * 1e-3) / 1e9
+    peak, peak_kind = measured_peaks()
+    traffic, traffic_src = profiled_traffic(args.workload)
+    cpu = None
+    if world == 1 and not args.no_cpu_baseline:
+        v, cores, desc = cpu_sample(wl, grid, cfg, flags, bc, tau, args.cpu_seconds)
+        cpu = {"value": round(v, 3), "unit": "MLUPs", "cores": cores, "kind": "port",
+               "sample": f"float32 CPU oracle on {desc} of the same workload"}
+    line = {
+        "metric": "D3Q19 MLUPs" if wl["lattice"] == "D3Q19" else f"{wl['lattice']} MLUPs",
+        "value": round(mlups, 2), "unit": "MLUPs", "n_gpus": world, "steps": K, "warmup": args.warmup,
+        "ms_per_step": round(t_ms / K, 5), "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+        "dtype": "f16c" if wl["f16"] else "f32", "data": "synthetic (lid-driven cavity from rest)",
+        "config": {"workload": wl["desc"], "grid": [grid.nx, grid.ny, grid.nz], "tile": list(grid.tile_shape),
+                   "layout": "reference tiled layout (col-major tile, col-major tiler)", "tau": round(tau, 6),
+                   "timing": "CUDA events around a K-step graph replay on the launching stream",
+                   "l2": "no flush: the two lattices (2 x %.2f GB) exceed the 129 MB L2" % (N * Q * (2 if wl["f16"] else 4) / 1e9),
+                   "parallelism": f"replicas x{world}" if world > 1 else "single GPU"},
+        "roofline": {"bound": "hbm", "achieved": round(achieved, 1), "peak": peak, "unit": "GB/s",
+                     "frac": round(achieved / peak, 4), "traffic": traffic,
+                     "note": f"{b_alg} B/update x {N} cells / median per-launch CUDA-event time {launch_ms:.4f} ms; "
+                             f"peak {peak_kind} (MEASURED_PEAKS.json hbm_gbs); traffic = ncu dram bytes per launch "
+                             f"({traffic_src or 'no capture committed'})"},
+        "cpu_baseline": cpu,
+        "e2e": {"value": round(e2e_mlups, 2), "unit": "MLUPs", "h2d_bytes_per_step": int(h2d / K),
+                "d2h_bytes_per_step": int(d2h / K),
+                "note": "Solver.run from pinned host buffers: upload of f, bc, flags and download of f inside the "
+                        f"timed region, amortised over the {K} steps"},
+        "gpu_launches": K,
+        "clocks": clk,
+    }
+    print(json.dumps(line), flush=True)
+    solver.close()
+    if world > 1:
+        import torch.distributed as dist
+        dist.destroy_process_group()
+    return line
+
+
+def run_reference(args, wl: dict):
+    """The reference arm: the reference's CPU path is not runnable here (Mojo), so its restatement
+    (the float32 CPU oracle, OpenMP over all host threads) runs on bounded slabs of the workload."""
+    rank, world, _ = dist_env()
+    if rank != 0:
+        return None
+    grid, cfg, flags, bc, tau = build_case(wl)
+    import oracle
+    N, Q = grid.num_points, grid.Q
+    f = np.zeros(N * Q, oracle.f_dtype(cfg, 32))
+    oracle.init(cfg, grid, 32, f)
+    f2 = f.copy() if wl["method"] == "db" else f
+    cores = oracle.max_threads()
+    slab = max(1, N // 64)
+    times = []
+    for k in range(args.warmup + args.steps):
+        b = (k * slab) % N
+        t0 = time.perf_counter()
+        oracle.step_range(cfg, grid, 32, f2, f, bc, flags, tau, k % 2 == 0, b, min(N, b + slab), cores)
+        dt = time.perf_counter() - t0
+        if k >= args.warmup:
+            times.append(dt)
+    t = sum(times)
+    v = slab * len(times) / t / 1e6
+    line = {"impl": "reference", "metric": "D3Q19 MLUPs" if wl["lattice"] == "D3Q19" else f"{wl['lattice']} MLUPs",
+            "value": round(v, 3), "unit": "MLUPs", "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
+            "ms_per_step": round(1e3 * t / len(times), 4), "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f16c" if wl["f16"] else "f32", "data": "synthetic (lid-driven cavity)",
+            "config": {"workload": wl["desc"], "grid": [grid.nx, grid.ny, grid.nz], "tile": list(grid.tile_shape),
+                       "step_sample": f"each step updates one slab of {slab} cells (1/64 of the grid)"},
+            "cpu_baseline": {"value": round(v, 3), "unit": "MLUPs", "cores": cores, "kind": "port",
+                             "sample": f"float32 CPU oracle (restatement of the reference step), {len(times)} "
+                                       f"slab-steps of {slab} cells; the reference itself is Mojo and not runnable"},
+            "e2e": {"value": round(v, 3), "unit": "MLUPs", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+    return line
+
+
+def main(argv=None):
+    ap = argparse.ArgumentParser(description=__doc__.splitlines()[0])
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=1000)
+    ap.add_argument("--warmup", type=int, default=64)
+    ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
+    ap.add_argument("--workload", choices=sorted(WORKLOADS), default=DEFAULT_WORKLOAD)
+    ap.add_argument("--threads", type=int, default=0, help="threads per block (0 = built-in)")
+    ap.add_argument("--cpu-seconds", type=float, default=12.0)
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    args = ap.parse_args(argv)
+    if args.warmup < 3:
+        ap.error("--warmup must be at least 3")
+    wl = WORKLOADS[args.workload]
+    if args.impl == "reference":
+        return run_reference(args, wl)
+    return run_ours(args, wl)
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,212 @@
+/*
+ * lbm_gb300.h — C ABI of the GB300 (sm_103a) fused lattice-Boltzmann stream–collide step.
+ *
+ * This library replaces the compute path of JohnCSu/mojo_lbm: the comptime-specialised Mojo
+ * GPU kernels `double_buffer_kernel` (src/lbm/kernels/double_buffer.mojo:25-99) and
+ * `esoteric_pull_kernel` (src/lbm/kernels/esoteric_pull.mojo:24-111), the host launch wrappers
+ * `Solver.double_buffer_step` / `Solver.esoteric_pull_step` (src/lbm/solver.mojo:81-154), the
+ * link-wise interpolated bounce-back kernel (src/lbm/geometry/interpolated_BB.mojo:46-141) and
+ * the output kernels that read the step's populations (src/lbm/output/velocity.mojo:25,
+ * src/lbm/output/drag.mojo:16).
+ *
+ * Conventions
+ *  - Every buffer argument is a caller-owned DEVICE pointer, laid out exactly as the reference's
+ *    tiled TileTensor layouts (src/lbm/layoutstruct.mojo:37-92):
+ *        f[x,y,z,q]  at  lx + tx*(ly + ty*(lz + tz*(q + Q*(bx + ntx*(by + nty*bz)))))
+ *        bc[x,y,z,k] at  the same formula with Q -> D+1 (k = 0..D-1 velocity, k = D density)
+ *        flags[x,y,z] at lx + tx*(ly + ty*lz) + tx*ty*tz*(bx + ntx*(by + nty*bz))
+ *    with lx = x % tx, bx = x / tx (same for y, z).  A tile equal to the whole grid
+ *    (tx,ty,tz) = (nx,ny,nz) is the reference's untiled column-major layout.
+ *  - Populations are float32, or uint16 Float16C codes when use_float16c is set.  The boundary
+ *    tensor bc is always float32.  Arithmetic is float32.
+ *  - `stream` is a cudaStream_t passed as void*; NULL is the legacy default stream.  All compute
+ *    calls are asynchronous on that stream unless they return a host value.
+ *  - Functions return an lbm_status; the message of the last failure on the calling thread is
+ *    returned by lbm_last_error().  Nothing traps or aborts on the device.
+ *  - A handle is not thread-safe; distinct handles are independent.
+ */
+#ifndef LBM_GB300_H
+#define LBM_GB300_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ---- status codes (the reference raises Error strings, src/lbm/assembly.mojo:115-189) ---- */
+typedef enum lbm_status {
+    LBM_OK = 0,
+    LBM_EINVAL = 1,       /* invalid argument or configuration                               */
+    LBM_ECUDA = 2,        /* a CUDA runtime call failed                                      */
+    LBM_ENAN = 3,         /* a reduction found a non-finite value                            */
+    LBM_ETIMEOUT = 4,     /* a bounded device wait gave up                                   */
+    LBM_ENOMEM = 5,       /* a handle-owned allocation failed                                */
+    LBM_EUNSUPPORTED = 6  /* the combination is not built (e.g. IBB with esoteric pull)      */
+} lbm_status;
+
+/* LBM_method (src/lbm/constants.mojo:20-31) */
+enum { LBM_DOUBLE_BUFFER = 0, LBM_ESOTERIC_PULL = 1 };
+
+/* Collisions (src/lbm/constants.mojo:41-55) */
+enum { LBM_SRT = 0, LBM_TRT = 1, LBM_KBC = 2, LBM_RLBM = 3 };
+
+/* lattices: get_D2Q9 / get_D3Q19 / get_D3Q27 (src/lbm/lattice.mojo:122,221,302) */
+enum { LBM_D2Q9 = 0, LBM_D3Q19 = 1, LBM_D3Q27 = 2 };
+
+/* Flags (src/lbm/constants.mojo:58-116): low nibble is an enum, high bits a bitmask */
+enum {
+    LBM_FLAG_FLUID = 0,
+    LBM_FLAG_SOLID = 1,
+    LBM_FLAG_EQUILIBRIUM = 2,
+    LBM_FLAG_FLUID_SOLID_BOUNDARY = 3,
+    LBM_FLAG_CAPTURE_VELOCITY = 0x20,
+    LBM_FLAG_CAPTURE_DENSITY = 0x40,
+    LBM_FLAG_EXCLUDE = 0x80
+};
+
+/* Bounceback_method (src/lbm/constants.mojo:120-123) */
+enum { LBM_BB_MID_GRID = 0, LBM_BB_BOUZIDI = 1 };
+
+/*
+ * lbm_config_t mirrors LBM_Config (src/lbm/config.mojo:50-153).  The reference fixes these at
+ * compile time; here they select a template instantiation at lbm_create.
+ *   include_equilibrium_bc  <=>  Flags.EQUILIBRIUM in config.INCLUDED_BCs (config.mojo:141-151)
+ *   Cs          Smagorinsky constant; the reference hard-codes 0.1 (steps/collide.mojo:200)
+ *   trt_lambda  TRT magic parameter; the reference hard-codes 3/16 (steps/collide.mojo:214)
+ * Fill with lbm_config_default() before changing fields.
+ */
+typedef struct lbm_config_t {
+    int32_t lbm_method;
+    int32_t collision_op;
+    int32_t LES;
+    int32_t DDF_shift;
+    int32_t use_float16c;
+    int32_t include_moving_boundary;
+    int32_t include_equilibrium_bc;
+    int32_t capture_density;
+    int32_t capture_velocity;
+    float Cs;
+    float trt_lambda;
+} lbm_config_t;
+
+/* lbm_grid_t mirrors LBM_Grid's comptime shape and tile (src/lbm/grid.mojo:55-107). */
+typedef struct lbm_grid_t {
+    int32_t lattice;           /* LBM_D2Q9 / LBM_D3Q19 / LBM_D3Q27                 */
+    int32_t nx, ny, nz;        /* nz == 1 for D2Q9                                  */
+    int32_t tx, ty, tz;        /* tile shape; each must divide its extent           */
+} lbm_grid_t;
+
+typedef struct lbm_handle lbm_handle;
+
+/* ---- configuration ---- */
+
+/* LBM_Config.__init__ defaults (config.mojo:85-99) for the given method. */
+lbm_status lbm_config_default(lbm_config_t* cfg, int32_t lbm_method);
+
+/* Host-only validation of a (config, grid) pair; needs no GPU.  The reference enforces the
+ * same rules with comptime asserts (config.mojo:153, grid.mojo:301-305,345-365,434-438,
+ * kernels/esoteric_pull.mojo:76-78). */
+lbm_status lbm_validate(const lbm_config_t* cfg, const lbm_grid_t* grid);
+
+/* Number of populations / spatial dimension of a lattice id, or -1. */
+int32_t lbm_lattice_q(int32_t lattice);
+int32_t lbm_lattice_d(int32_t lattice);
+
+/* Element count of f / bc / flags for the grid (Q*N, (D+1)*N, N). */
+int64_t lbm_f_elements(const lbm_grid_t* grid);
+int64_t lbm_bc_elements(const lbm_grid_t* grid);
+int64_t lbm_flag_elements(const lbm_grid_t* grid);
+
+/* ---- handle ---- */
+
+/* Solver.__init__ (solver.mojo:63-76): validates and selects the kernel for the current device. */
+lbm_status lbm_create(const lbm_config_t* cfg, const lbm_grid_t* grid, lbm_handle** out);
+lbm_status lbm_destroy(lbm_handle* h);
+
+/* Solver(block_dim=...) override (solver.mojo:63-76): threads per block (multiple of 32,
+ * 32..1024) or 0 for the built-in choice. */
+lbm_status lbm_set_block_threads(lbm_handle* h, int32_t threads);
+
+/* ---- the step ---- */
+
+/* Solver.double_buffer_step (solver.mojo:81-111) -> double_buffer_kernel
+ * (kernels/double_buffer.mojo:25-99): one pull step f_in -> f_out.  bc is written only when
+ * capture_density / capture_velocity are set. */
+lbm_status lbm_double_buffer_step(lbm_handle* h, void* f_out, const void* f_in, float* bc,
+                                  const uint8_t* flags, float tau, void* stream);
+
+/* Solver.esoteric_pull_step[is_even_step] (solver.mojo:115-154) -> esoteric_pull_kernel
+ * (kernels/esoteric_pull.mojo:24-111): one in-place step.  The initial state is stored with
+ * the odd-step pattern, so the first step after initialisation is even. */
+lbm_status lbm_esoteric_pull_step(lbm_handle* h, void* f, float* bc, const uint8_t* flags,
+                                  float tau, int32_t is_even_step, void* stream);
+
+/* The host time loop of examples/LDC.mojo:133-135 as one call: n_steps steps replayed from a
+ * CUDA graph captured per (buffers, tau, parity).  Double buffer: step k reads f_a when
+ * (first_step + k) is even, else f_b.  Esoteric pull: f_b is ignored and step k is even when
+ * (first_step + k) is even. */
+lbm_status lbm_run(lbm_handle* h, void* f_a, void* f_b, float* bc, const uint8_t* flags,
+                   float tau, int64_t n_steps, int64_t first_step, void* stream);
+
+/* ---- set-up and outputs ---- */
+
+/* initialize_f_from_func / initialize_fluid_at_rest (preprocess/initial_condition.mojo:47-234):
+ * f = f_eq(rho, u) (+ f_neq from the velocity gradient when grad != NULL), stored with the
+ * double-buffer pattern or, for esoteric pull, the odd-step pattern.
+ * u: [D][nx][ny][nz] floats (row-major, as the reference's velocity_layout, examples/LDC.mojo:48),
+ * lattice units (NULL = at rest).  grad: [D*D][nx][ny][nz] floats, du_a/dx_b at component a*D+b
+ * (NULL = no non-equilibrium part). */
+lbm_status lbm_init_equilibrium(lbm_handle* h, void* f, float rho, float tau, const float* u,
+                                const float* grad, void* stream);
+
+/* calculate_rho_and_velocity (output/velocity.mojo:25-125).  rho: [nx][ny][nz] floats and
+ * u: [D][nx][ny][nz] floats, row-major as the reference's density_layout / velocity_layout
+ * (examples/LDC.mojo:47-48).  For esoteric pull, after_odd_step selects the load pattern
+ * (ignored for double buffer). */
+lbm_status lbm_compute_rho_u(lbm_handle* h, float* rho, float* u, const void* f, const float* bc,
+                             const uint8_t* flags, int32_t after_odd_step, void* stream);
+
+/* Mass and momentum of all non-solid, non-excluded cells, reduced in float64 on the device:
+ * out = {sum rho, sum rho*u_x, sum rho*u_y, sum rho*u_z}.  Synchronises the stream.
+ * Returns LBM_ENAN if any reduced value is not finite. */
+lbm_status lbm_reduce_mass_momentum(lbm_handle* h, const void* f, const uint8_t* flags,
+                                    int32_t after_odd_step, double out[4], void* stream);
+
+/* linkwise_bounceback_kernel (geometry/interpolated_BB.mojo:46-141) as launched by
+ * RigidStationaryObject.bounceback (geometry/rigidstationary.mojo:127-153): per link, in place
+ * on the lattice the last double-buffer step wrote.  fluid_ids are linear flag-layout indices,
+ * dirs the direction pointing into the wall, dists the wall distance q in [0,1].
+ * link_force (n_links*D floats, link fastest) is written when compute_force != 0.
+ * method: LBM_BB_MID_GRID or LBM_BB_BOUZIDI. */
+lbm_status lbm_linkwise_bounceback(lbm_handle* h, void* f, float* link_force,
+                                   const int32_t* fluid_ids, const int32_t* dirs,
+                                   const float* dists, int64_t n_links, int32_t method,
+                                   int32_t compute_force, float q_clamp, void* stream);
+
+/* RigidStationaryObject.sum_force (geometry/rigidstationary.mojo:155-169): column sums of a
+ * link-force array, reduced in float64 on the device.  Synchronises the stream. */
+lbm_status lbm_sum_link_force(lbm_handle* h, const float* link_force, int64_t n_links,
+                              double out[3], void* stream);
+
+/* calculate_drag_around_object (output/drag.mojo:16-105): momentum-exchange force per listed
+ * fluid node (n_nodes*D floats, node fastest). */
+lbm_status lbm_drag_force(lbm_handle* h, float* node_force, const void* f, const uint8_t* flags,
+                          const int32_t* fluid_ids, int64_t n_nodes, void* stream);
+
+/* Float16C codec (src/utils/custom_fp.mojo:36-101) over device arrays. */
+lbm_status lbm_float16c_encode(const float* in, uint16_t* out, int64_t n, void* stream);
+lbm_status lbm_float16c_decode(const uint16_t* in, float* out, int64_t n, void* stream);
+
+/* Message of the last failed call on this thread ("" if none). */
+const char* lbm_last_error(void);
+
+/* Library version string. */
+const char* lbm_version(void);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* LBM_GB300_H */

@@ -1,0 +1,508 @@
+// C ABI of the GB300 LBM step (include/lbm_gb300.h): configuration checks, handles, dispatch to
+// the per-lattice kernel tables, the graph-replayed time loop, and the auxiliary kernels.
+#include <cuda_runtime.h>
+
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <map>
+#include <mutex>
+#include <string>
+#include <tuple>
+
+#include "lbm_aux.cuh"
+
+namespace lbm {
+StepLaunch get_step_d2q9(int, int, int, int);
+StepLaunch get_step_d3q19(int, int, int, int);
+StepLaunch get_step_d3q27(int, int, int, int);
+}  // namespace lbm
+
+using namespace lbm;
+
+namespace {
+
+thread_local std::string g_err;
+
+lbm_status fail(lbm_status s, const std::string& msg) {
+    g_err = msg;
+    return s;
+}
+
+#define LBM_CK(call)                                                                          \
+    do {                                                                                      \
+        cudaError_t e_ = (call);                                                              \
+        if (e_ != cudaSuccess)                                                                \
+            return fail(LBM_ECUDA, std::string(#call) + ": " + cudaGetErrorString(e_));       \
+    } while (0)
+
+int lattice_q(int id) { return id == LBM_D2Q9 ? 9 : id == LBM_D3Q19 ? 19 : id == LBM_D3Q27 ? 27 : -1; }
+int lattice_d(int id) { return id == LBM_D2Q9 ? 2 : (id == LBM_D3Q19 || id == LBM_D3Q27) ? 3 : -1; }
+
+// Graph cache key for lbm_run: buffers, tau bits, parity of the first step, chunk length.
+using GraphKey = std::tuple<const void*, const void*, const void*, const void*, uint32_t, int, int64_t>;
+
+}  // namespace
+
+struct lbm_handle {
+    lbm_config_t cfg;
+    lbm_grid_t grid;
+    LayoutDesc lay;
+    StepLaunch step;
+    int threads;
+    int device;
+    int sm_count;
+    double* scratch;  // kReduceBlocks*4 partials + 4 results
+    cudaStream_t capture_stream;
+    std::map<GraphKey, cudaGraphExec_t> graphs;
+};
+
+namespace {
+
+LayoutDesc make_layout(const lbm_grid_t& g) {
+    LayoutDesc l;
+    l.nx = g.nx; l.ny = g.ny; l.nz = g.nz;
+    l.tx = g.tx; l.ty = g.ty; l.tz = g.tz;
+    l.ntx = g.nx / g.tx; l.nty = g.ny / g.ty; l.ntz = g.nz / g.tz;
+    l.T = (uint32_t)(g.tx * g.ty * g.tz);
+    l.ncells = (uint32_t)((int64_t)g.nx * g.ny * g.nz);
+    l.d_tx = FastDiv((uint32_t)g.tx);
+    l.d_ty = FastDiv((uint32_t)g.ty);
+    l.d_T = FastDiv(l.T);
+    l.d_ntx = FastDiv((uint32_t)l.ntx);
+    l.d_nty = FastDiv((uint32_t)l.nty);
+    return l;
+}
+
+StepArgs step_args(const lbm_handle* h, const void* f_in, void* f_out, float* bc, const uint8_t* flags, float tau,
+                   int even) {
+    StepArgs a;
+    a.lay = h->lay;
+    a.f_in = f_in;
+    a.f_out = f_out;
+    a.bc = bc;
+    a.flags = flags;
+    a.tau = tau;
+    a.Cs = h->cfg.Cs;
+    a.trt_lambda = h->cfg.trt_lambda;
+    a.ddf = h->cfg.DDF_shift;
+    a.moving = h->cfg.include_moving_boundary;
+    a.eqbc = h->cfg.include_equilibrium_bc;
+    a.cap_rho = h->cfg.capture_density;
+    a.cap_u = h->cfg.capture_velocity;
+    a.even = even;
+    return a;
+}
+
+uint32_t blocks_for(uint32_t n, int threads) { return (n + (uint32_t)threads - 1u) / (uint32_t)threads; }
+
+lbm_status check_handle(const lbm_handle* h) {
+    if (!h) return fail(LBM_EINVAL, "null handle");
+    return LBM_OK;
+}
+
+lbm_status step_once(lbm_handle* h, const void* f_in, void* f_out, float* bc, const uint8_t* flags, float tau,
+                     int even, cudaStream_t s) {
+    const StepArgs a = step_args(h, f_in, f_out, bc, flags, tau, even);
+    LBM_CK(h->step(a, h->threads, s));
+    return LBM_OK;
+}
+
+template <class F>
+lbm_status dispatch_lattice(int lattice, F&& f) {
+    switch (lattice) {
+        case LBM_D2Q9: return f(D2Q9{});
+        case LBM_D3Q19: return f(D3Q19{});
+        case LBM_D3Q27: return f(D3Q27{});
+    }
+    return fail(LBM_EINVAL, "unknown lattice");
+}
+
+}  // namespace
+
+extern "C" {
+
+const char* lbm_last_error(void) { return g_err.c_str(); }
+
+const char* lbm_version(void) { return "mojo_lbm_gb300 0.1 (sm_103a)"; }
+
+int32_t lbm_lattice_q(int32_t lattice) { return lattice_q(lattice); }
+int32_t lbm_lattice_d(int32_t lattice) { return lattice_d(lattice); }
+
+int64_t lbm_f_elements(const lbm_grid_t* g) {
+    return g ? (int64_t)lattice_q(g->lattice) * g->nx * g->ny * g->nz : -1;
+}
+int64_t lbm_bc_elements(const lbm_grid_t* g) {
+    return g ? (int64_t)(lattice_d(g->lattice) + 1) * g->nx * g->ny * g->nz : -1;
+}
+int64_t lbm_flag_elements(const lbm_grid_t* g) { return g ? (int64_t)g->nx * g->ny * g->nz : -1; }
+
+lbm_status lbm_config_default(lbm_config_t* cfg, int32_t lbm_method) {
+    if (!cfg) return fail(LBM_EINVAL, "null config");
+    if (lbm_method != LBM_DOUBLE_BUFFER && lbm_method != LBM_ESOTERIC_PULL)
+        return fail(LBM_EINVAL, "lbm_method must be LBM_DOUBLE_BUFFER or LBM_ESOTERIC_PULL");
+    std::memset(cfg, 0, sizeof(*cfg));
+    cfg->lbm_method = lbm_method;
+    cfg->collision_op = LBM_SRT;
+    cfg->include_moving_boundary = 1;
+    cfg->Cs = 0.1f;
+    cfg->trt_lambda = 3.0f / 16.0f;
+    return LBM_OK;
+}
+
+lbm_status lbm_validate(const lbm_config_t* c, const lbm_grid_t* g) {
+    if (!c || !g) return fail(LBM_EINVAL, "null config or grid");
+    if (c->lbm_method != LBM_DOUBLE_BUFFER && c->lbm_method != LBM_ESOTERIC_PULL)
+        return fail(LBM_EINVAL, "lbm_method not valid");
+    /* Collisions.valid_set (constants.mojo:53) */
+    if (c->collision_op < LBM_SRT || c->collision_op > LBM_RLBM)
+        return fail(LBM_EINVAL, "Invalid Collision Operator specified: must be SRT, TRT, KBC or RLBM");
+    const int D = lattice_d(g->lattice);
+    if (D < 0) return fail(LBM_EINVAL, "lattice must be LBM_D2Q9, LBM_D3Q19 or LBM_D3Q27");
+    if (g->nx <= 0 || g->ny <= 0 || g->nz <= 0) return fail(LBM_EINVAL, "grid extents must be positive");
+    /* check_model_match_dim (grid.mojo:345-365) */
+    const int gridD = (g->nx > 1) + (g->ny > 1) + (g->nz > 1);
+    if (gridD != D)
+        return fail(LBM_EINVAL,
+                    "The given dimension of the Lattice does not match that of the dimension of the grid");
+    if (g->tx <= 0 || g->ty <= 0 || g->tz <= 0) return fail(LBM_EINVAL, "tile extents must be positive");
+    /* set_block_shape_and_grid_dim / set_grid_dims (grid.mojo:301-305,434-438) */
+    if (g->nx % g->tx || g->ny % g->ty || g->nz % g->tz)
+        return fail(LBM_EINVAL, "Tile size must divide nx, ny and nz");
+    const int64_t N = (int64_t)g->nx * g->ny * g->nz;
+    if (N >= (int64_t)1 << 32) return fail(LBM_EINVAL, "grid has 2^32 or more cells");
+    if (c->use_float16c && !(c->Cs == c->Cs)) return fail(LBM_EINVAL, "Cs is NaN");
+    if (c->LES && !(c->Cs >= 0.0f)) return fail(LBM_EINVAL, "Cs must be non-negative");
+    return LBM_OK;
+}
+
+lbm_status lbm_create(const lbm_config_t* cfg, const lbm_grid_t* grid, lbm_handle** out) {
+    if (!out) return fail(LBM_EINVAL, "null output handle pointer");
+    *out = nullptr;
+    lbm_status s = lbm_validate(cfg, grid);
+    if (s != LBM_OK) return s;
+    lbm_handle* h = new lbm_handle();
+    h->cfg = *cfg;
+    h->grid = *grid;
+    h->lay = make_layout(*grid);
+    const int m = cfg->lbm_method, f16 = cfg->use_float16c ? 1 : 0, co = cfg->collision_op, les = cfg->LES ? 1 : 0;
+    h->step = grid->lattice == LBM_D2Q9 ? get_step_d2q9(m, f16, co, les)
+            : grid->lattice == LBM_D3Q19 ? get_step_d3q19(m, f16, co, les)
+                                         : get_step_d3q27(m, f16, co, les);
+    h->threads = 256;
+    h->scratch = nullptr;
+    h->capture_stream = nullptr;
+    cudaError_t e = cudaGetDevice(&h->device);
+    if (e == cudaSuccess) e = cudaDeviceGetAttribute(&h->sm_count, cudaDevAttrMultiProcessorCount, h->device);
+    if (e == cudaSuccess) e = cudaMalloc(&h->scratch, sizeof(double) * (kReduceBlocks * kReduceWidth + 8));
+    if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&h->capture_stream, cudaStreamNonBlocking);
+    if (e != cudaSuccess) {
+        lbm_destroy(h);
+        return fail(LBM_ECUDA, std::string("lbm_create: ") + cudaGetErrorString(e));
+    }
+    *out = h;
+    return LBM_OK;
+}
+
+lbm_status lbm_destroy(lbm_handle* h) {
+    if (!h) return LBM_OK;
+    for (auto& kv : h->graphs) cudaGraphExecDestroy(kv.second);
+    if (h->scratch) cudaFree(h->scratch);
+    if (h->capture_stream) cudaStreamDestroy(h->capture_stream);
+    delete h;
+    return LBM_OK;
+}
+
+lbm_status lbm_set_block_threads(lbm_handle* h, int32_t threads) {
+    if (check_handle(h)) return LBM_EINVAL;
+    if (threads == 0) threads = 256;
+    if (threads < 32 || threads > 256 || threads % 32)
+        return fail(LBM_EINVAL, "threads per block must be a multiple of 32 in [32, 256]");
+    h->threads = threads;
+    return LBM_OK;
+}
+
+lbm_status lbm_double_buffer_step(lbm_handle* h, void* f_out, const void* f_in, float* bc, const uint8_t* flags,
+                                  float tau, void* stream) {
+    if (check_handle(h)) return LBM_EINVAL;
+    if (h->cfg.lbm_method != LBM_DOUBLE_BUFFER)
+        return fail(LBM_EINVAL, "This function is only valid if the lbm method is Double Buffer");
+    if (!f_out || !f_in || !flags) return fail(LBM_EINVAL, "null buffer");
+    if (f_out == f_in) return fail(LBM_EINVAL, "double buffer step needs distinct f_in and f_out");
+    if (!bc && (h->cfg.include_moving_boundary || h->cfg.include_equilibrium_bc || h->cfg.capture_density ||
+                h->cfg.capture_velocity))
+        return fail(LBM_EINVAL, "bc is required by this configuration");
+    return step_once(h, f_in, f_out, bc, flags, tau, 0, (cudaStream_t)stream);
+}
+
+lbm_status lbm_esoteric_pull_step(lbm_handle* h, void* f, float* bc, const uint8_t* flags, float tau,
+                                  int32_t is_even_step, void* stream) {
+    if (check_handle(h)) return LBM_EINVAL;
+    if (h->cfg.lbm_method != LBM_ESOTERIC_PULL)
+        return fail(LBM_EINVAL, "This function is only valid if the lbm method is Esoteric Pull");
+    if (!f || !flags) return fail(LBM_EINVAL, "null buffer");
+    if (!bc && (h->cfg.include_moving_boundary || h->cfg.include_equilibrium_bc || h->cfg.capture_density ||
+                h->cfg.capture_velocity))
+        return fail(LBM_EINVAL, "bc is required by this configuration");
+    return step_once(h, f, f, bc, flags, tau, is_even_step ? 1 : 0, (cudaStream_t)stream);
+}
+
+lbm_status lbm_run(lbm_handle* h, void* f_a, void* f_b, float* bc, const uint8_t* flags, float tau, int64_t n_steps,
+                   int64_t first_step, void* stream) {
+    if (check_handle(h)) return LBM_EINVAL;
+    if (n_steps < 0 || first_step < 0) return fail(LBM_EINVAL, "n_steps and first_step must be non-negative");
+    const bool eso = h->cfg.lbm_method == LBM_ESOTERIC_PULL;
+    if (!f_a || !flags || (!eso && (!f_b || f_a == f_b))) return fail(LBM_EINVAL, "bad buffers for lbm_run");
+    if (!bc && (h->cfg.include_moving_boundary || h->cfg.include_equilibrium_bc || h->cfg.capture_density ||
+                h->cfg.capture_velocity))
+        return fail(LBM_EINVAL, "bc is required by this configuration");
+    cudaStream_t s = (cudaStream_t)stream;
+    auto launch_k = [&](int64_t k) -> lbm_status {
+        const bool a_is_src = ((first_step + k) % 2) == 0;
+        if (eso) return step_once(h, f_a, f_a, bc, flags, tau, a_is_src ? 1 : 0, s);
+        return a_is_src ? step_once(h, f_a, f_b, bc, flags, tau, 0, s) : step_once(h, f_b, f_a, bc, flags, tau, 0, s);
+    };
+    // Chunks of an even number of steps keep the buffer/parity pattern of every replay identical.
+    const int64_t chunk = 64;
+    int64_t done = 0;
+    if (n_steps >= chunk) {
+        uint32_t tau_bits;
+        std::memcpy(&tau_bits, &tau, 4);
+        const GraphKey key{f_a, f_b, bc, flags, tau_bits, (int)(first_step % 2), chunk};
+        auto it = h->graphs.find(key);
+        if (it == h->graphs.end()) {
+            cudaGraph_t g = nullptr;
+            LBM_CK(cudaStreamBeginCapture(h->capture_stream, cudaStreamCaptureModeThreadLocal));
+            lbm_status st = LBM_OK;
+            for (int64_t k = 0; k < chunk && st == LBM_OK; ++k) {
+                const bool a_is_src = ((first_step + k) % 2) == 0;
+                const StepArgs a = eso ? step_args(h, f_a, f_a, bc, flags, tau, a_is_src ? 1 : 0)
+                                       : (a_is_src ? step_args(h, f_a, f_b, bc, flags, tau, 0)
+                                                   : step_args(h, f_b, f_a, bc, flags, tau, 0));
+                if (h->step(a, h->threads, h->capture_stream) != cudaSuccess) st = LBM_ECUDA;
+            }
+            cudaError_t e = cudaStreamEndCapture(h->capture_stream, &g);
+            if (st != LBM_OK || e != cudaSuccess) {
+                if (g) cudaGraphDestroy(g);
+                return fail(LBM_ECUDA, "lbm_run: graph capture failed");
+            }
+            cudaGraphExec_t ge = nullptr;
+            e = cudaGraphInstantiate(&ge, g, 0);
+            cudaGraphDestroy(g);
+            if (e != cudaSuccess) return fail(LBM_ECUDA, std::string("lbm_run: ") + cudaGetErrorString(e));
+            it = h->graphs.emplace(key, ge).first;
+        }
+        for (; done + chunk <= n_steps; done += chunk) LBM_CK(cudaGraphLaunch(it->second, s));
+    }
+    for (; done < n_steps; ++done) {
+        const lbm_status st = launch_k(done);
+        if (st != LBM_OK) return st;
+    }
+    return LBM_OK;
+}
+
+lbm_status lbm_init_equilibrium(lbm_handle* h, void* f, float rho, float tau, const float* u, const float* grad,
+                                void* stream) {
+    if (check_handle(h)) return LBM_EINVAL;
+    if (!f) return fail(LBM_EINVAL, "null f");
+    InitArgs a;
+    a.lay = h->lay;
+    a.f = f;
+    a.u = u;
+    a.grad = grad;
+    a.rho = rho;
+    a.tau = tau;
+    a.ddf = h->cfg.DDF_shift;
+    a.esoteric = h->cfg.lbm_method == LBM_ESOTERIC_PULL;
+    const bool f16 = h->cfg.use_float16c != 0;
+    cudaStream_t s = (cudaStream_t)stream;
+    const uint32_t nb = blocks_for(h->lay.ncells, 256);
+    return dispatch_lattice(h->grid.lattice, [&](auto Lt) -> lbm_status {
+        using L = decltype(Lt);
+        if (f16) init_kernel<L, true><<<nb, 256, 0, s>>>(a);
+        else init_kernel<L, false><<<nb, 256, 0, s>>>(a);
+        LBM_CK(cudaGetLastError());
+        return LBM_OK;
+    });
+}
+
+lbm_status lbm_compute_rho_u(lbm_handle* h, float* rho, float* u, const void* f, const float* bc,
+                             const uint8_t* flags, int32_t after_odd_step, void* stream) {
+    if (check_handle(h)) return LBM_EINVAL;
+    if (!rho || !u || !f || !bc || !flags) return fail(LBM_EINVAL, "null buffer");
+    RhoUArgs a;
+    a.lay = h->lay;
+    a.f = f;
+    a.bc = bc;
+    a.flags = flags;
+    a.rho = rho;
+    a.u = u;
+    a.ddf = h->cfg.DDF_shift;
+    a.moving = h->cfg.include_moving_boundary;
+    a.eqbc = h->cfg.include_equilibrium_bc;
+    a.even = after_odd_step ? 1 : 0;
+    const bool f16 = h->cfg.use_float16c != 0, eso = h->cfg.lbm_method == LBM_ESOTERIC_PULL;
+    cudaStream_t s = (cudaStream_t)stream;
+    const uint32_t nb = blocks_for(h->lay.ncells, 256);
+    return dispatch_lattice(h->grid.lattice, [&](auto Lt) -> lbm_status {
+        using L = decltype(Lt);
+        if (f16) {
+            if (eso) rho_u_kernel<L, true, true><<<nb, 256, 0, s>>>(a);
+            else rho_u_kernel<L, true, false><<<nb, 256, 0, s>>>(a);
+        } else {
+            if (eso) rho_u_kernel<L, false, true><<<nb, 256, 0, s>>>(a);
+            else rho_u_kernel<L, false, false><<<nb, 256, 0, s>>>(a);
+        }
+        LBM_CK(cudaGetLastError());
+        return LBM_OK;
+    });
+}
+
+lbm_status lbm_reduce_mass_momentum(lbm_handle* h, const void* f, const uint8_t* flags, int32_t after_odd_step,
+                                    double out[4], void* stream) {
+    if (check_handle(h)) return LBM_EINVAL;
+    if (!f || !flags || !out) return fail(LBM_EINVAL, "null buffer");
+    MassArgs a;
+    a.lay = h->lay;
+    a.f = f;
+    a.flags = flags;
+    a.partial = h->scratch;
+    a.ddf = h->cfg.DDF_shift;
+    a.even = after_odd_step ? 1 : 0;
+    const bool f16 = h->cfg.use_float16c != 0, eso = h->cfg.lbm_method == LBM_ESOTERIC_PULL;
+    cudaStream_t s = (cudaStream_t)stream;
+    lbm_status st = dispatch_lattice(h->grid.lattice, [&](auto Lt) -> lbm_status {
+        using L = decltype(Lt);
+        if (f16) {
+            if (eso) mass_partial_kernel<L, true, true><<<kReduceBlocks, kReduceThreads, 0, s>>>(a);
+            else mass_partial_kernel<L, true, false><<<kReduceBlocks, kReduceThreads, 0, s>>>(a);
+        } else {
+            if (eso) mass_partial_kernel<L, false, true><<<kReduceBlocks, kReduceThreads, 0, s>>>(a);
+            else mass_partial_kernel<L, false, false><<<kReduceBlocks, kReduceThreads, 0, s>>>(a);
+        }
+        LBM_CK(cudaGetLastError());
+        return LBM_OK;
+    });
+    if (st != LBM_OK) return st;
+    double* res = h->scratch + kReduceBlocks * kReduceWidth;
+    final_sum_kernel<4><<<1, kReduceThreads, 0, s>>>(h->scratch, kReduceBlocks, res);
+    LBM_CK(cudaGetLastError());
+    LBM_CK(cudaMemcpyAsync(out, res, 4 * sizeof(double), cudaMemcpyDeviceToHost, s));
+    LBM_CK(cudaStreamSynchronize(s));
+    for (int k = 0; k < 4; ++k)
+        if (!std::isfinite(out[k])) return fail(LBM_ENAN, "mass/momentum reduction found a non-finite value");
+    return LBM_OK;
+}
+
+lbm_status lbm_linkwise_bounceback(lbm_handle* h, void* f, float* link_force, const int32_t* fluid_ids,
+                                   const int32_t* dirs, const float* dists, int64_t n_links, int32_t method,
+                                   int32_t compute_force, float q_clamp, void* stream) {
+    if (check_handle(h)) return LBM_EINVAL;
+    if (h->cfg.lbm_method != LBM_DOUBLE_BUFFER)
+        return fail(LBM_EUNSUPPORTED, "linkwise bounce-back needs the double-buffer method");
+    if (method != LBM_BB_MID_GRID && method != LBM_BB_BOUZIDI) return fail(LBM_EINVAL, "unknown bounce-back method");
+    if (n_links < 0) return fail(LBM_EINVAL, "n_links must be non-negative");
+    if (n_links == 0) return LBM_OK;
+    if (!f || !fluid_ids || !dirs || !dists || (compute_force && !link_force)) return fail(LBM_EINVAL, "null buffer");
+    LinkArgs a;
+    a.lay = h->lay;
+    a.f = f;
+    a.force = link_force;
+    a.ids = fluid_ids;
+    a.dirs = dirs;
+    a.dists = dists;
+    a.n = n_links;
+    a.q_clamp = q_clamp;
+    a.bouzidi = method == LBM_BB_BOUZIDI;
+    a.compute_force = compute_force;
+    a.ddf = h->cfg.DDF_shift;
+    const bool f16 = h->cfg.use_float16c != 0;
+    cudaStream_t s = (cudaStream_t)stream;
+    const uint32_t nb = (uint32_t)((n_links + 255) / 256);
+    return dispatch_lattice(h->grid.lattice, [&](auto Lt) -> lbm_status {
+        using L = decltype(Lt);
+        if (f16) link_kernel<L, true><<<nb, 256, 0, s>>>(a);
+        else link_kernel<L, false><<<nb, 256, 0, s>>>(a);
+        LBM_CK(cudaGetLastError());
+        return LBM_OK;
+    });
+}
+
+lbm_status lbm_sum_link_force(lbm_handle* h, const float* link_force, int64_t n_links, double out[3], void* stream) {
+    if (check_handle(h)) return LBM_EINVAL;
+    if (!out || (n_links > 0 && !link_force)) return fail(LBM_EINVAL, "null buffer");
+    if (n_links < 0) return fail(LBM_EINVAL, "n_links must be non-negative");
+    out[0] = out[1] = out[2] = 0.0;
+    if (n_links == 0) return LBM_OK;
+    cudaStream_t s = (cudaStream_t)stream;
+    const int D = lattice_d(h->grid.lattice);
+    colsum_partial_kernel<<<kReduceBlocks, kReduceThreads, 0, s>>>(link_force, n_links, D, h->scratch);
+    LBM_CK(cudaGetLastError());
+    double* res = h->scratch + kReduceBlocks * kReduceWidth;
+    final_sum_kernel<4><<<1, kReduceThreads, 0, s>>>(h->scratch, kReduceBlocks, res);
+    LBM_CK(cudaGetLastError());
+    double tmp[4];
+    LBM_CK(cudaMemcpyAsync(tmp, res, 4 * sizeof(double), cudaMemcpyDeviceToHost, s));
+    LBM_CK(cudaStreamSynchronize(s));
+    for (int k = 0; k < 3; ++k) out[k] = tmp[k];
+    return LBM_OK;
+}
+
+lbm_status lbm_drag_force(lbm_handle* h, float* node_force, const void* f, const uint8_t* flags,
+                          const int32_t* fluid_ids, int64_t n_nodes, void* stream) {
+    if (check_handle(h)) return LBM_EINVAL;
+    if (n_nodes < 0) return fail(LBM_EINVAL, "n_nodes must be non-negative");
+    if (n_nodes == 0) return LBM_OK;
+    if (!node_force || !f || !flags || !fluid_ids) return fail(LBM_EINVAL, "null buffer");
+    DragArgs a;
+    a.lay = h->lay;
+    a.f = f;
+    a.flags = flags;
+    a.ids = fluid_ids;
+    a.force = node_force;
+    a.n = n_nodes;
+    a.ddf = h->cfg.DDF_shift;
+    const bool f16 = h->cfg.use_float16c != 0;
+    cudaStream_t s = (cudaStream_t)stream;
+    const uint32_t nb = (uint32_t)((n_nodes + 255) / 256);
+    return dispatch_lattice(h->grid.lattice, [&](auto Lt) -> lbm_status {
+        using L = decltype(Lt);
+        if (f16) drag_kernel<L, true><<<nb, 256, 0, s>>>(a);
+        else drag_kernel<L, false><<<nb, 256, 0, s>>>(a);
+        LBM_CK(cudaGetLastError());
+        return LBM_OK;
+    });
+}
+
+}  // extern "C"
+
+namespace {
+__global__ void f16c_encode_kernel(const float* in, uint16_t* out, int64_t n) {
+    const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n) out[i] = (uint16_t)f16c_encode(in[i]);
+}
+__global__ void f16c_decode_kernel(const uint16_t* in, float* out, int64_t n) {
+    const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n) out[i] = f16c_decode(in[i]);
+}
+}  // namespace
+
+extern "C" {
+
+lbm_status lbm_float16c_encode(const float* in, uint16_t* out, int64_t n, void* stream) {
+    if (n < 0 || (n > 0 && (!in || !out))) return fail(LBM_EINVAL, "bad codec arguments");
+    if (n == 0) return LBM_OK;
+    f16c_encode_kernel<<<(unsigned)((n + 255) / 256), 256, 0, (cudaStream_t)stream>>>(in, out, n);
+    LBM_CK(cudaGetLastError());
+    return LBM_OK;
+}
+
+lbm_status lbm_float16c_decode(const uint16_t* in, float* out, int64_t n, void* stream) {
+    if (n < 0 || (n > 0 && (!in || !out))) return fail(LBM_EINVAL, "bad codec arguments");
+    if (n == 0) return LBM_OK;
+    f16c_decode_kernel<<<(unsigned)((n + 255) / 256), 256, 0, (cudaStream_t)stream>>>(in, out, n);
+    LBM_CK(cudaGetLastError());
+    return LBM_OK;
+}
+
+}  // extern "C"

@@ -1,0 +1,419 @@
+// The fused stream–collide step for sm_103a.
+//
+// One thread per lattice cell, threads in the memory order of the reference's tiled layout
+// (src/lbm/layoutstruct.mojo:37-92), so every own-cell population access of a warp is a
+// contiguous 128-byte (float32) or 64-byte (Float16C) run.  A cell does, in order:
+//   stream   — double_buffer_pull_load_f_vec / esoteric_pull_load_f_vec
+//              (src/lbm/kernels/ops/load_and_store.mojo:11-86,164-221)
+//   BC       — moving_wall_bc, equilibrium_bc (src/lbm/kernels/ops/boundary_condition.mojo:17-205)
+//   collide  — SRT / TRT / RLBM / KBC with optional Smagorinsky LES
+//              (src/lbm/kernels/steps/collide.mojo:23-90)
+//   store    — store_f_vec_to_global (src/lbm/kernels/steps/store_f.mojo:13-40)
+// The kernel is bound by HBM traffic (Q loads + Q stores per cell); all arithmetic stays in
+// registers, unrolled at compile time over q as the reference does with `comptime for`.
+#pragma once
+
+#include "lbm_device.cuh"
+
+namespace lbm {
+
+struct StepArgs {
+    LayoutDesc lay;
+    const void* f_in;
+    void* f_out;          // == f_in for esoteric pull
+    float* bc;
+    const uint8_t* flags;
+    float tau, Cs, trt_lambda;
+    int32_t ddf, moving, eqbc, cap_rho, cap_u, even;
+};
+
+// Storage traits: float32, or Float16C codes decoded to float32 (load_f / store_f,
+// src/lbm/kernels/utils/load_and_store.mojo:17-110).
+template <bool F16C> struct Pop;
+template <> struct Pop<false> {
+    using T = float;
+    static __device__ __forceinline__ float ld(const float* p) { return __ldg(p); }
+    static __device__ __forceinline__ float ld_rw(const float* p) { return *p; }
+    static __device__ __forceinline__ void st(float* p, float v) { *p = v; }
+};
+template <> struct Pop<true> {
+    using T = uint16_t;
+    static __device__ __forceinline__ float ld(const uint16_t* p) { return f16c_decode(__ldg(p)); }
+    static __device__ __forceinline__ float ld_rw(const uint16_t* p) { return f16c_decode(*p); }
+    static __device__ __forceinline__ void st(uint16_t* p, float v) { *p = (uint16_t)f16c_encode(v); }
+};
+
+// Neighbour offsets along one axis for shifts -1, 0, +1 with the periodic wrap of
+// get_adjacent_idx (src/lbm/kernels/utils/index.mojo:44-64): the local part (already scaled by
+// the in-tile stride) and the tile part (scaled by the tile stride of the tiler).
+struct Axis {
+    uint32_t loc[3], til[3];
+    __device__ __forceinline__ void init(uint32_t l, uint32_t b, uint32_t t, uint32_t nt, uint32_t lstride,
+                                         uint32_t tstride) {
+        loc[1] = l * lstride;
+        til[1] = b * tstride;
+        if (l > 0u) { loc[0] = (l - 1u) * lstride; til[0] = til[1]; }
+        else { loc[0] = (t - 1u) * lstride; til[0] = (b > 0u ? b - 1u : nt - 1u) * tstride; }
+        if (l + 1u < t) { loc[2] = (l + 1u) * lstride; til[2] = til[1]; }
+        else { loc[2] = 0u; til[2] = (b + 1u < nt ? b + 1u : 0u) * tstride; }
+    }
+};
+
+struct Nbr {
+    Axis ax, ay, az;
+    // neighbour at (x + sx, y + sy, z + sz), sx..sz in {-1,0,1}: (loc, tile)
+    template <int SX, int SY, int SZ>
+    __device__ __forceinline__ uint32_t loc() const { return ax.loc[SX + 1] + ay.loc[SY + 1] + az.loc[SZ + 1]; }
+    template <int SX, int SY, int SZ>
+    __device__ __forceinline__ uint32_t til() const { return ax.til[SX + 1] + ay.til[SY + 1] + az.til[SZ + 1]; }
+};
+
+template <class L>
+__device__ __forceinline__ float edot(const float* u, int q) {
+    // dot(velocity, direction) in d order, zero terms skipped (they add +-0)
+    float o = 0.f;
+    if (L::c(q, 0)) o = L::c(q, 0) > 0 ? o + u[0] : o - u[0];
+    if (L::c(q, 1)) o = L::c(q, 1) > 0 ? o + u[1] : o - u[1];
+    if constexpr (L::D == 3) if (L::c(q, 2)) o = L::c(q, 2) > 0 ? o + u[2] : o - u[2];
+    return o;
+}
+
+// f_eq (src/lbm/kernels/utils/equilibrium.mojo:10-39)
+template <class L, int q>
+__device__ __forceinline__ float feq(float rho, const float* u, float uu, bool ddf) {
+    constexpr float w = wf<L>(q);
+    const float eu = edot<L>(u, q);
+    if (ddf) return w * rho * (3.f * eu + 4.5f * eu * eu - 1.5f * uu) + w * (rho - 1.f);
+    return w * rho * (1.f + 3.f * eu + 4.5f * eu * eu - 1.5f * uu);
+}
+
+// KBC shear part of the deviatoric non-equilibrium stress.  D2Q9 is get_shear_D2Q9
+// (src/lbm/kernels/ops/collisions/KBC_.mojo:137-175); the 3D form is the same projection for
+// D3Q19/D3Q27 (Karlin, Bösch, Chikatamarla, PRE 90, 031302, 2014).
+template <class L, int q>
+__device__ __forceinline__ float kbc_shear(const float* P) {
+    constexpr int cx = L::c(q, 0), cy = L::c(q, 1), cz = L::c(q, 2);
+    constexpr int nnz = (cx != 0) + (cy != 0) + (cz != 0);
+    if constexpr (L::D == 2) {
+        const float N = P[0] - P[2];
+        if constexpr (nnz == 1) return cx != 0 ? N * 0.25f : -N * 0.25f;
+        else if constexpr (nnz == 2) return (cx * cy > 0) ? P[1] * 0.25f : -P[1] * 0.25f;
+        else return 0.f;
+    } else {
+        if constexpr (nnz == 1) {
+            const float Nxz = P[0] - P[5], Nyz = P[3] - P[5];
+            constexpr float sixth = (float)(1.0 / 6.0);
+            if constexpr (cx != 0) return (2.f * Nxz - Nyz) * sixth;
+            else if constexpr (cy != 0) return (2.f * Nyz - Nxz) * sixth;
+            else return (-Nxz - Nyz) * sixth;
+        } else if constexpr (nnz == 2) {
+            if constexpr (cz == 0) return (float)(cx * cy) * P[1] * 0.25f;
+            else if constexpr (cy == 0) return (float)(cx * cz) * P[2] * 0.25f;
+            else return (float)(cy * cz) * P[4] * 0.25f;
+        } else {
+            return 0.f;
+        }
+    }
+}
+
+// collide (src/lbm/kernels/steps/collide.mojo:23-90)
+template <class L, int COLL, bool LES>
+__device__ __forceinline__ void collide(float (&f)[L::Q], float tau, const StepArgs& a, float* bc_own_base,
+                                        uint32_t T, uint8_t own_flag) {
+    constexpr int Q = L::Q, D = L::D;
+    const bool ddf = a.ddf != 0;
+    float rho = 0.f;
+    static_for<0, Q>([&](auto qc) { rho += f[qc.value]; });
+    if (ddf) rho += 1.f;
+    float mom[3] = {0.f, 0.f, 0.f};
+    static_for<0, Q>([&](auto qc) {
+        constexpr int q = qc.value;
+        static_for<0, D>([&](auto dc) {
+            constexpr int d = dc.value;
+            if constexpr (L::c(q, d) > 0) mom[d] += f[q];
+            else if constexpr (L::c(q, d) < 0) mom[d] -= f[q];
+        });
+    });
+    float u[3] = {0.f, 0.f, 0.f};
+    static_for<0, D>([&](auto dc) { u[dc.value] = mom[dc.value] / rho; });
+    float uu = 0.f;
+    static_for<0, D>([&](auto dc) { uu += u[dc.value] * u[dc.value]; });
+
+    if (a.cap_rho && (own_flag & LBM_FLAG_CAPTURE_DENSITY)) bc_own_base[(size_t)T * D] = rho;
+    if (a.cap_u && (own_flag & LBM_FLAG_CAPTURE_VELOCITY))
+        static_for<0, D>([&](auto dc) { bc_own_base[(size_t)T * dc.value] = u[dc.value]; });
+
+    float tau_local = tau;
+    constexpr bool NEED_NEQ = LES || COLL == LBM_KBC || COLL == LBM_RLBM;
+    if constexpr (NEED_NEQ) {
+        // get_non_eq_second_order_moment (src/lbm/kernels/utils/moment.mojo:111-150)
+        float P[L::NS];
+        static_for<0, L::NS>([&](auto nc) { P[nc.value] = 0.f; });
+        static_for<0, Q>([&](auto qc) {
+            constexpr int q = qc.value;
+            const float fn = f[q] - feq<L, q>(rho, u, uu, ddf);
+            static_for<0, L::NS>([&](auto nc) {
+                constexpr int n = nc.value;
+                constexpr int cc = L::c(q, sa<L>(n)) * L::c(q, sb<L>(n));
+                if constexpr (cc > 0) P[n] += fn;
+                else if constexpr (cc < 0) P[n] -= fn;
+            });
+        });
+        if constexpr (LES) {
+            // get_strain_rate_tensor / _norm_squared (moment.mojo:154-215),
+            // get_Smagorinsky_LES_tau (src/lbm/kernels/ops/turbulence.mojo:12-38)
+            const float k = -1.f / (2.f * rho * (float)(1.0 / 3.0) * tau_local);
+            float s2 = 0.f;
+            static_for<0, L::NS>([&](auto nc) {
+                constexpr int n = nc.value;
+                const float S = P[n] * k;
+                if constexpr (sa<L>(n) != sb<L>(n)) s2 += (S * S) * 2.f;
+                else s2 += S * S;
+            });
+            tau_local += 3.f * ((a.Cs * a.Cs) * sqrtf(2.f * s2));
+        }
+        if constexpr (COLL == LBM_RLBM) {
+            // RLBM (src/lbm/kernels/ops/collisions/collision.mojo:168-223)
+            const float one_m = 1.f - 1.f / tau_local;
+            static_for<0, Q>([&](auto qc) {
+                constexpr int q = qc.value;
+                float dot = 0.f;
+                static_for<0, L::NS>([&](auto nc) {
+                    constexpr int n = nc.value, A = sa<L>(n), B = sb<L>(n);
+                    constexpr float Qn = (A == B) ? (float)(L::c(q, A) * L::c(q, B)) - (float)(1.0 / 3.0)
+                                                  : (float)(2 * L::c(q, A) * L::c(q, B));
+                    if constexpr (Qn != 0.f) dot += Qn * P[n];
+                });
+                constexpr float k = (float)(L::wd(q) / (2.0 / 9.0));
+                f[q] = feq<L, q>(rho, u, uu, ddf) + one_m * (k * dot);
+            });
+        } else if constexpr (COLL == LBM_KBC) {
+            // KBC (src/lbm/kernels/ops/collisions/KBC_.mojo:180-238); gamma is not clamped
+            const float beta = 1.f / (2.f * tau_local);
+            const float inv_beta = 2.f * tau_local;
+            float sp1 = 0.f, sp2 = 0.f;
+            static_for<0, Q>([&](auto qc) {
+                constexpr int q = qc.value;
+                const float fe0 = feq<L, q>(rho, u, uu, false);
+                const float ds = kbc_shear<L, q>(P);
+                const float dh = (f[q] - feq<L, q>(rho, u, uu, ddf)) - ds;
+                sp1 += ds * dh / fe0;
+                sp2 += dh * dh / fe0;
+            });
+            const float gamma = inv_beta - (2.f - inv_beta) * sp1 / (sp2 + 1e-32f);
+            static_for<0, Q>([&](auto qc) {
+                constexpr int q = qc.value;
+                const float ds = kbc_shear<L, q>(P);
+                const float dh = (f[q] - feq<L, q>(rho, u, uu, ddf)) - ds;
+                f[q] -= beta * (2.f * ds + gamma * dh);
+            });
+        }
+    }
+    if constexpr (COLL == LBM_SRT) {
+        // SRT (src/lbm/kernels/ops/collisions/collision.mojo:12-46)
+        const float inv_tau = 1.f / tau_local;
+        static_for<0, Q>([&](auto qc) {
+            constexpr int q = qc.value;
+            f[q] -= inv_tau * (f[q] - feq<L, q>(rho, u, uu, ddf));
+        });
+    } else if constexpr (COLL == LBM_TRT) {
+        // TRT (collision.mojo:49-113) with tau_asymm of steps/collide.mojo:214-215
+        const float tau_a = 0.5f + a.trt_lambda / (tau_local - 0.5f);
+        const float is = 1.f / tau_local, ia = 1.f / tau_a;
+        f[0] -= is * (f[0] - feq<L, 0>(rho, u, uu, ddf));
+        static_for<1, Q, 2>([&](auto qc) {
+            constexpr int q = qc.value, o = q + 1;
+            const float fs = (f[q] + f[o]) * 0.5f, fa = (f[q] - f[o]) * 0.5f;
+            const float eq = feq<L, q>(rho, u, uu, ddf), eo = feq<L, o>(rho, u, uu, ddf);
+            const float es = (eq + eo) * 0.5f, ea = (eq - eo) * 0.5f;
+            const float sym = is * (fs - es);
+            f[q] -= (sym + ia * (fa - ea));
+            f[o] -= (sym + ia * ((-fa) - (-ea)));
+        });
+    }
+}
+
+template <class L, int METHOD, bool F16C, int COLL, bool LES>
+__global__ void __launch_bounds__(256) step_kernel(const StepArgs a) {
+    using P = Pop<F16C>;
+    using S = typename P::T;
+    constexpr int Q = L::Q, D = L::D, K = D + 1;
+    constexpr bool ESO = METHOD == LBM_ESOTERIC_PULL;
+
+    const uint32_t n = blockIdx.x * blockDim.x + threadIdx.x;
+    if (n >= a.lay.ncells) return;
+    const uint8_t flag = __ldg(a.flags + n);
+    // is_valid_thread (src/lbm/kernels/utils/checks.mojo:55-60)
+    if ((flag & 0x0F) == LBM_FLAG_SOLID || (flag & LBM_FLAG_EXCLUDE)) return;
+
+    const uint32_t T = a.lay.T;
+    const uint32_t tile = a.lay.d_T.div(n);
+    const uint32_t loc = n - tile * T;
+    const uint32_t lyz = a.lay.d_tx.div(loc);
+    const uint32_t lx = loc - lyz * (uint32_t)a.lay.tx;
+    const uint32_t lz = a.lay.d_ty.div(lyz);
+    const uint32_t ly = lyz - lz * (uint32_t)a.lay.ty;
+    const uint32_t byz = a.lay.d_ntx.div(tile);
+    const uint32_t bx = tile - byz * (uint32_t)a.lay.ntx;
+    const uint32_t bz = a.lay.d_nty.div(byz);
+    const uint32_t by = byz - bz * (uint32_t)a.lay.nty;
+
+    Nbr nb;
+    const uint32_t txy = (uint32_t)(a.lay.tx * a.lay.ty);
+    const uint32_t ntxy = (uint32_t)(a.lay.ntx * a.lay.nty);
+    nb.ax.init(lx, bx, a.lay.tx, a.lay.ntx, 1u, 1u);
+    nb.ay.init(ly, by, a.lay.ty, a.lay.nty, (uint32_t)a.lay.tx, (uint32_t)a.lay.ntx);
+    if constexpr (D == 3) nb.az.init(lz, bz, a.lay.tz, a.lay.ntz, txy, ntxy);
+    else { nb.az.loc[0] = nb.az.loc[1] = nb.az.loc[2] = 0u; nb.az.til[0] = nb.az.til[1] = nb.az.til[2] = 0u; }
+
+    const uint64_t TQ = (uint64_t)T * Q;
+    const S* fin = (const S*)a.f_in;
+    S* fout = (S*)a.f_out;
+    const uint64_t own = loc + TQ * tile;
+
+    // ---- neighbour flags at x - c_q (set_adjacent_flags, ops/load_and_store.mojo:270-291)
+    uint32_t raw_solid = 0u, nib_solid = 0u;
+    const bool need_flags = !ESO || a.moving;
+    if (need_flags) {
+        static_for<1, Q>([&](auto qc) {
+            constexpr int q = qc.value;
+            constexpr int sx = -L::c(q, 0), sy = -L::c(q, 1), sz = -L::c(q, 2);
+            const uint32_t m = nb.template loc<sx, sy, sz>() + T * nb.template til<sx, sy, sz>();
+            const uint8_t pf = __ldg(a.flags + m);
+            if (pf == LBM_FLAG_SOLID) raw_solid |= 1u << q;
+            if ((pf & 0x0F) == LBM_FLAG_SOLID) nib_solid |= 1u << q;
+        });
+    }
+
+    // ---- stream
+    float f[Q];
+    if constexpr (!ESO) {
+        static_for<0, Q>([&](auto qc) {
+            constexpr int q = qc.value;
+            constexpr int sx = -L::c(q, 0), sy = -L::c(q, 1), sz = -L::c(q, 2);
+            const uint64_t pull = nb.template loc<sx, sy, sz>() + TQ * nb.template til<sx, sy, sz>() + (uint64_t)T * q;
+            const uint64_t bounce = own + (uint64_t)T * opp<L>(q);
+            // mid-grid bounce-back on a raw SOLID compare (ops/load_and_store.mojo:216)
+            f[q] = P::ld(fin + ((raw_solid >> q) & 1u ? bounce : pull));
+        });
+    } else {
+        const bool ev = a.even != 0;
+        f[0] = P::ld_rw(fin + own);
+        static_for<1, Q - 1, 2>([&](auto qc) {
+            constexpr int pos = qc.value, neg = pos + 1;
+            constexpr int sx = L::c(pos, 0), sy = L::c(pos, 1), sz = L::c(pos, 2);
+            const uint64_t nbase = nb.template loc<sx, sy, sz>() + TQ * nb.template til<sx, sy, sz>();
+            const uint32_t sA = ev ? pos : neg, sB = ev ? neg : pos;
+            f[pos] = P::ld_rw(fin + own + (uint64_t)T * sA);
+            f[neg] = P::ld_rw(fin + nbase + (uint64_t)T * sB);
+        });
+    }
+
+    // ---- boundary conditions (steps/apply_boundary_condition.mojo:10-41)
+    if (a.moving && nib_solid) {
+        const float* bc = a.bc;
+        const uint64_t TK = (uint64_t)T * K;
+        static_for<1, Q>([&](auto qc) {
+            constexpr int q = qc.value;
+            if ((nib_solid >> q) & 1u) {
+                constexpr int sx = -L::c(q, 0), sy = -L::c(q, 1), sz = -L::c(q, 2);
+                const uint64_t b = nb.template loc<sx, sy, sz>() + TK * nb.template til<sx, sy, sz>();
+                float cu = 0.f;
+                static_for<0, D>([&](auto dc) {
+                    constexpr int d = dc.value;
+                    if constexpr (L::c(q, d) > 0) cu += bc[b + (uint64_t)T * d];
+                    else if constexpr (L::c(q, d) < 0) cu -= bc[b + (uint64_t)T * d];
+                });
+                constexpr float six_w = 6.f * wf<L>(q);
+                f[q] += six_w * bc[b + (uint64_t)T * D] * cu;
+            }
+        });
+    }
+    const uint64_t own_bc = loc + (uint64_t)T * K * tile;
+    if (a.eqbc && (flag & 0x0F) == LBM_FLAG_EQUILIBRIUM) {
+        const bool ddf = a.ddf != 0;
+        const float* bc = a.bc;
+        float ub[3] = {0.f, 0.f, 0.f};
+        static_for<0, D>([&](auto dc) { ub[dc.value] = bc[own_bc + (uint64_t)T * dc.value]; });
+        const float rb = bc[own_bc + (uint64_t)T * D];
+        const int32_t gx = (int32_t)(bx * a.lay.tx + lx), gy = (int32_t)(by * a.lay.ty + ly),
+                      gz = (int32_t)(bz * a.lay.tz + lz);
+        const int32_t g[3] = {gx, gy, gz}, ng[3] = {a.lay.nx, a.lay.ny, a.lay.nz};
+        float rl = 0.f, ul[3] = {0.f, 0.f, 0.f};
+        static_for<0, Q>([&](auto qc) {
+            constexpr int q = qc.value;
+            bool oob = false;
+            static_for<0, D>([&](auto dc) {
+                constexpr int d = dc.value;
+                const int32_t pi = g[d] - L::c(q, d);
+                oob = oob || pi < 0 || pi >= ng[d];
+            });
+            const float fq = oob ? (ddf ? 0.f : wf<L>(q)) : f[q];
+            rl += fq;
+            static_for<0, D>([&](auto dc) {
+                constexpr int d = dc.value;
+                if constexpr (L::c(q, d) > 0) ul[d] += fq;
+                else if constexpr (L::c(q, d) < 0) ul[d] -= fq;
+            });
+        });
+        if (ddf) rl += 1.f;
+        static_for<0, D>([&](auto dc) { ul[dc.value] = ul[dc.value] / rl; });
+        const bool ufree = isnan(ub[0]);
+        float us[3];
+        static_for<0, D>([&](auto dc) { us[dc.value] = ufree ? ul[dc.value] : ub[dc.value]; });
+        const float rs = isnan(rb) ? rl : rb;
+        float uu = 0.f;
+        static_for<0, D>([&](auto dc) { uu += us[dc.value] * us[dc.value]; });
+        static_for<0, Q>([&](auto qc) { f[qc.value] = feq<L, qc.value>(rs, us, uu, ddf); });
+    }
+
+    collide<L, COLL, LES>(f, a.tau, a, a.bc + own_bc, T, flag);
+
+    // ---- store
+    if constexpr (!ESO) {
+        static_for<0, Q>([&](auto qc) { P::st(fout + own + (uint64_t)T * qc.value, f[qc.value]); });
+    } else {
+        // esoteric_pull_store_f_vec (ops/load_and_store.mojo:89-159): the same slots as loaded
+        const bool ev = a.even != 0;
+        P::st(fout + own, f[0]);
+        static_for<1, Q - 1, 2>([&](auto qc) {
+            constexpr int pos = qc.value, neg = pos + 1;
+            constexpr int sx = L::c(pos, 0), sy = L::c(pos, 1), sz = L::c(pos, 2);
+            const uint64_t nbase = nb.template loc<sx, sy, sz>() + TQ * nb.template til<sx, sy, sz>();
+            const uint32_t sA = ev ? pos : neg, sB = ev ? neg : pos;
+            P::st(fout + nbase + (uint64_t)T * sB, f[pos]);
+            P::st(fout + own + (uint64_t)T * sA, f[neg]);
+        });
+    }
+}
+
+// Launcher type used by the dispatch tables.
+using StepLaunch = cudaError_t (*)(const StepArgs&, int threads, cudaStream_t);
+
+template <class L, int METHOD, bool F16C, int COLL, bool LES>
+cudaError_t launch_step(const StepArgs& a, int threads, cudaStream_t s) {
+    const uint32_t blocks = (a.lay.ncells + (uint32_t)threads - 1u) / (uint32_t)threads;
+    step_kernel<L, METHOD, F16C, COLL, LES><<<blocks, threads, 0, s>>>(a);
+    return cudaGetLastError();
+}
+
+// Table of the 32 variants of one lattice, indexed by
+// ((method*2 + f16c)*4 + collision)*2 + les.
+template <class L>
+struct StepTable {
+    static StepLaunch get(int method, int f16c, int coll, int les) {
+        static const StepLaunch t[32] = {
+#define LBM_ROW(M, F)                                                                         \
+    &launch_step<L, M, F, LBM_SRT, false>, &launch_step<L, M, F, LBM_SRT, true>,              \
+        &launch_step<L, M, F, LBM_TRT, false>, &launch_step<L, M, F, LBM_TRT, true>,          \
+        &launch_step<L, M, F, LBM_KBC, false>, &launch_step<L, M, F, LBM_KBC, true>,          \
+        &launch_step<L, M, F, LBM_RLBM, false>, &launch_step<L, M, F, LBM_RLBM, true>
+            LBM_ROW(LBM_DOUBLE_BUFFER, false), LBM_ROW(LBM_DOUBLE_BUFFER, true),
+            LBM_ROW(LBM_ESOTERIC_PULL, false), LBM_ROW(LBM_ESOTERIC_PULL, true)
+#undef LBM_ROW
+        };
+        return t[((method * 2 + f16c) * 4 + coll) * 2 + les];
+    }
+};
+
+}  // namespace lbm

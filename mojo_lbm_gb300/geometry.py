@@ -1,0 +1,106 @@
+"""Immersed sphere/circle geometry and its bounce-back links
+(mirrors src/lbm/geometry/rigidSphere.mojo:14-170 and rigidstationary.mojo:21-169).
+
+Link discovery is host set-up (numpy); the bounce-back itself and the force sum run on the
+device through the library.
+"""
+from __future__ import annotations
+
+import numpy as np
+import torch
+
+from .constants import Flags
+
+
+def get_q_for_sphere(xf: np.ndarray, xs: np.ndarray, center: np.ndarray, radius: float) -> np.ndarray:
+    """Link parameter t in [0, 1] where the segment xf -> xs meets the sphere
+    (rigidSphere.mojo:132-170)."""
+    f2c = xf - center
+    s2f = xs - xf
+    a = (s2f * s2f).sum(-1)
+    b = (f2c * s2f).sum(-1) * 2
+    c = (f2c * f2c).sum(-1) - radius * radius
+    sq = np.sqrt(b * b - 4 * a * c)
+    t1 = (-b + sq) / (2 * a)
+    t2 = (-b - sq) / (2 * a)
+    return np.where((t1 >= 0.0) & (t1 <= 1.0), t1, t2)
+
+
+class RigidStationaryObject:
+    """Link lists of one stationary body: fluid node (flag-layout index), direction into the
+    wall, wall distance."""
+
+    def __init__(self, grid, unique_fluid_ids, fluid_boundaries, lattice_links, link_distances, device="cuda"):
+        self.grid = grid
+        self.unique_fluid_ids = np.asarray(unique_fluid_ids, dtype=np.int32)
+        self.fluid_boundaries_list = np.asarray(fluid_boundaries, dtype=np.int32)
+        self.lattice_links_list = np.asarray(lattice_links, dtype=np.int32)
+        self.link_distances_list = np.asarray(link_distances, dtype=np.float32)
+        n = len(self.fluid_boundaries_list)
+        if len(self.lattice_links_list) != n or len(self.link_distances_list) != n:
+            raise ValueError("links_fluid_list, links_direction_list and links_q_dist, should all be the same length")
+        dev = torch.device(device)
+        self.fluid_boundaries = torch.as_tensor(self.fluid_boundaries_list, device=dev)
+        self.lattice_links = torch.as_tensor(self.lattice_links_list, device=dev)
+        self.link_distances = torch.as_tensor(self.link_distances_list, device=dev)
+        self.link_forces = torch.zeros(max(n, 1) * grid.D, dtype=torch.float32, device=dev)
+
+    def num_links(self) -> int:
+        return len(self.fluid_boundaries_list)
+
+    def bounceback(self, solver, f, method: int, compute_force: bool = True, q_min: float = 0.0, stream=None):
+        """RigidStationaryObject.bounceback (rigidstationary.mojo:127-153)."""
+        solver.linkwise_bounceback(f, self.link_forces, self.fluid_boundaries, self.lattice_links,
+                                   self.link_distances, method, compute_force, q_min, stream)
+
+    def sum_force(self, solver, *, in_lattice_units: bool = True, units=None):
+        """Float64 device sum of the link forces (rigidstationary.mojo:155-169)."""
+        F = solver.sum_link_force(self.link_forces, self.num_links())
+        if in_lattice_units:
+            return F
+        return tuple(units.force.C_lat_to_phys() * v for v in F)
+
+
+def get_rigid_sphere(grid, flags_host: np.ndarray, center, radius: float, device="cuda") -> RigidStationaryObject:
+    """Marks nodes inside the sphere SOLID in flags_host and collects the fluid-to-solid links
+    (rigidSphere.mojo:14-129).  Links are ordered by fluid node (x, y, z) then q."""
+    if len(center) != 3:
+        raise ValueError(f"centre must be a list of 3 floats got a len of {len(center)} instead")
+    D, Q = grid.D, grid.Q
+    c = np.asarray(center, dtype=np.float64)
+    lo, hi = [], []
+    for i in range(3):
+        if i < D:
+            a_min, a_max = c[i] - radius, c[i] + radius
+            lo.append(max(0, int((a_min - grid.origin[i]) // grid.dx) - 1))
+            hi.append(min(grid.shape[i], int((a_max - grid.origin[i]) // grid.dx + 1) + 1) + 1)
+        else:
+            lo.append(0)
+            hi.append(1)
+    rng = [np.arange(lo[i], min(hi[i], grid.shape[i])) for i in range(3)]
+    X, Y, Z = np.meshgrid(*rng, indexing="ij")
+    X, Y, Z = X.ravel(), Y.ravel(), Z.ravel()
+    P = np.stack(grid.get_grid_coordinates(X, Y, Z), -1)
+    inside = ((P - c) ** 2).sum(-1) <= radius ** 2
+    lay = grid.layouts
+    flags_host[lay.flag_offset(X[inside], Y[inside], Z[inside])] = Flags.SOLID
+    fx, fy, fz = X[~inside], Y[~inside], Z[~inside]
+    xf = P[~inside]
+    ids, dirs, dists, uniq = [], [], [], []
+    dirs_c = grid.lattice.directions
+    for k in range(len(fx)):
+        fid = int(lay.flag_offset(fx[k], fy[k], fz[k]))
+        first = True
+        for q in range(Q):
+            t = [fx[k], fy[k], fz[k]]
+            for i in range(D):
+                t[i] += int(dirs_c[q][i])
+            xs = np.asarray(grid.get_grid_coordinates(*t), dtype=np.float64)
+            if ((xs - c) ** 2).sum() <= radius ** 2:
+                if first:
+                    uniq.append(fid)
+                    first = False
+                ids.append(fid)
+                dirs.append(q)
+                dists.append(float(get_q_for_sphere(xf[k], xs, c, radius)))
+    return RigidStationaryObject(grid, uniq, ids, dirs, dists, device)

@@ -1,0 +1,148 @@
+"""TEST INFRASTRUCTURE — ctypes wrapper of the CPU oracle (liblbm_oracle.so).
+
+Only tests/, __graft_entry__.smoke() and bench.py's CPU-baseline leg import this module, as
+the checker or as the timed CPU reference; the product never does.  Parity with the reference
+is UNPINNED (see lbm_oracle.cpp): the reference is Mojo and its repository has no golden
+vectors for the step; the oracle is pinned to the Ghia et al. cavity fixture and invariants.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import subprocess
+from pathlib import Path
+
+import numpy as np
+
+HERE = Path(__file__).resolve().parent
+LIB = HERE / "liblbm_oracle.so"
+
+_lib = None
+
+
+def build(force: bool = False) -> Path:
+    """Compiles the oracle with its Makefile (g++, OpenMP)."""
+    src = [HERE / "lbm_oracle.cpp", HERE / "Makefile", HERE.parent / "include" / "lbm_gb300.h"]
+    if force or not LIB.exists() or any(p.stat().st_mtime > LIB.stat().st_mtime for p in src):
+        subprocess.run(["make", "-s", "-C", str(HERE), "-B" if force else "liblbm_oracle.so"], check=True)
+    return LIB
+
+
+def lib() -> C.CDLL:
+    global _lib
+    if _lib is None:
+        build()
+        h = C.CDLL(str(LIB))
+        vp, i32, i64, f64 = C.c_void_p, C.c_int, C.c_int64, C.c_double
+        h.oracle_step.argtypes = [vp, vp, i32, vp, vp, vp, vp, f64, i32, i32]
+        h.oracle_step_range.argtypes = [vp, vp, i32, vp, vp, vp, vp, f64, i32, i32, i64, i64]
+        h.oracle_init.argtypes = [vp, vp, i32, vp, f64, f64, vp, vp]
+        h.oracle_rho_u.argtypes = [vp, vp, i32, vp, vp, vp, vp, vp, i32]
+        h.oracle_links.argtypes = [vp, vp, i32, vp, vp, vp, vp, vp, i64, i32, i32, f64]
+        h.oracle_drag.argtypes = [vp, vp, i32, vp, vp, vp, vp, i64]
+        h.oracle_gather.argtypes = [vp, vp, i32, vp, vp, i32]
+        h.oracle_f16c_encode.argtypes = [vp, vp, i64]
+        h.oracle_f16c_decode.argtypes = [vp, vp, i64]
+        h.oracle_layout_offset.argtypes = [vp, i64, i64, i64, i64, i64]
+        h.oracle_layout_offset.restype = i64
+        h.oracle_lattice.argtypes = [i32, vp, vp, vp]
+        h.oracle_max_threads.restype = i32
+        _lib = h
+    return _lib
+
+
+def _p(a):
+    return None if a is None else a.ctypes.data
+
+
+def _cfg(cfg):
+    return C.byref(cfg.to_c()) if hasattr(cfg, "to_c") else C.byref(cfg)
+
+
+def f_dtype(cfg, prec: int):
+    if prec == 64:
+        return np.float64
+    return np.uint16 if cfg.use_float16c else np.float32
+
+
+def step(cfg, grid, prec: int, f_out, f_in, bc, flags, tau: float, is_even: bool = False, nthreads: int = 0):
+    """One step of the oracle.  prec 32: float32 arithmetic (Float16C storage when configured);
+    prec 64: float64 arithmetic and storage.  For esoteric pull pass f_out is f_in."""
+    g = grid.to_c()
+    lib().oracle_step(_cfg(cfg), C.byref(g), prec, _p(f_out), _p(f_in), _p(bc), _p(flags), float(tau),
+                      int(bool(is_even)), int(nthreads))
+
+
+def step_range(cfg, grid, prec: int, f_out, f_in, bc, flags, tau: float, is_even: bool, begin: int, end: int,
+               nthreads: int = 0):
+    """The step on the cells with index x + nx*(y + ny*z) in [begin, end) only."""
+    g = grid.to_c()
+    lib().oracle_step_range(_cfg(cfg), C.byref(g), prec, _p(f_out), _p(f_in), _p(bc), _p(flags), float(tau),
+                            int(bool(is_even)), int(nthreads), int(begin), int(end))
+
+
+def init(cfg, grid, prec: int, f, rho: float = 1.0, tau: float = 1.0, u=None, grad=None):
+    g = grid.to_c()
+    u64 = None if u is None else np.ascontiguousarray(u, dtype=np.float64)
+    g64 = None if grad is None else np.ascontiguousarray(grad, dtype=np.float64)
+    lib().oracle_init(_cfg(cfg), C.byref(g), prec, _p(f), float(rho), float(tau), _p(u64), _p(g64))
+
+
+def rho_u(cfg, grid, prec: int, f, bc, flags, after_odd: bool = False):
+    N, D = grid.num_points, grid.D
+    dt = np.float64 if prec == 64 else np.float32
+    rho = np.empty(N, dtype=dt)
+    u = np.empty(D * N, dtype=dt)
+    g = grid.to_c()
+    lib().oracle_rho_u(_cfg(cfg), C.byref(g), prec, _p(f), _p(bc), _p(flags), _p(rho), _p(u), int(bool(after_odd)))
+    return rho.reshape(grid.shape), u.reshape((D,) + grid.shape)
+
+
+def links(cfg, grid, prec: int, f, force, ids, dirs, dists, method: int, compute_force: bool, q_clamp: float):
+    g = grid.to_c()
+    lib().oracle_links(_cfg(cfg), C.byref(g), prec, _p(f), _p(force), _p(ids), _p(dirs), _p(dists), len(ids),
+                       int(method), int(bool(compute_force)), float(q_clamp))
+
+
+def drag(cfg, grid, prec: int, force, f, flags, ids):
+    g = grid.to_c()
+    lib().oracle_drag(_cfg(cfg), C.byref(g), prec, _p(force), _p(f), _p(flags), _p(ids), len(ids))
+
+
+def gather(cfg, grid, prec: int, f, after_odd: bool = False):
+    """[Q, nx, ny, nz] populations the next step would load (no boundary treatment)."""
+    dt = np.float64 if prec == 64 else np.float32
+    out = np.empty(grid.Q * grid.num_points, dtype=dt)
+    g = grid.to_c()
+    lib().oracle_gather(_cfg(cfg), C.byref(g), prec, _p(f), _p(out), int(bool(after_odd)))
+    return out.reshape((grid.Q,) + grid.shape)
+
+
+def f16c_encode(x: np.ndarray) -> np.ndarray:
+    x = np.ascontiguousarray(x, dtype=np.float32)
+    out = np.empty(x.shape, dtype=np.uint16)
+    lib().oracle_f16c_encode(_p(x), _p(out), x.size)
+    return out
+
+
+def f16c_decode(h: np.ndarray) -> np.ndarray:
+    h = np.ascontiguousarray(h, dtype=np.uint16)
+    out = np.empty(h.shape, dtype=np.float32)
+    lib().oracle_f16c_decode(_p(h), _p(out), h.size)
+    return out
+
+
+def layout_offset(grid, x, y, z, k, K) -> int:
+    g = grid.to_c()
+    return int(lib().oracle_layout_offset(C.byref(g), x, y, z, k, K))
+
+
+def lattice(lattice_id: int):
+    c = np.zeros(27 * 3, dtype=np.int32)
+    w = np.zeros(27, dtype=np.float64)
+    o = np.zeros(27, dtype=np.int32)
+    Q = lib().oracle_lattice(lattice_id, _p(c), _p(w), _p(o))
+    return c[: 3 * Q].reshape(Q, 3), w[:Q], o[:Q]
+
+
+def max_threads() -> int:
+    return int(lib().oracle_max_threads())
