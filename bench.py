@@ -359,12 +359,19 @@ def main(argv=None):
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
     ap.add_argument("--workload", choices=sorted(WORKLOADS), default=DEFAULT_WORKLOAD)
     ap.add_argument("--threads", type=int, default=0, help="threads per block (0 = built-in)")
+    ap.add_argument("--tile", type=str, default="", help="tile shape tx,ty,tz of the layout (default per workload)")
+    ap.add_argument("--n", type=int, default=0, help="cube edge override (profiling on a smaller case)")
     ap.add_argument("--cpu-seconds", type=float, default=12.0)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     args = ap.parse_args(argv)
     if args.warmup < 3:
         ap.error("--warmup must be at least 3")
-    wl = WORKLOADS[args.workload]
+    wl = dict(WORKLOADS[args.workload])
+    if args.tile:
+        wl["tile"] = tuple(int(v) for v in args.tile.split(","))
+    if args.n:
+        wl["n"] = args.n
+        wl["desc"] = wl["desc"].replace("256^3", f"{args.n}^3")
     if args.impl == "reference":
         return run_reference(args, wl)
     return run_ours(args, wl)

@@ -125,9 +125,18 @@ int64_t lbm_flag_elements(const lbm_grid_t* grid);
 lbm_status lbm_create(const lbm_config_t* cfg, const lbm_grid_t* grid, lbm_handle** out);
 lbm_status lbm_destroy(lbm_handle* h);
 
-/* Solver(block_dim=...) override (solver.mojo:63-76): threads per block (multiple of 32,
- * 32..1024) or 0 for the built-in choice. */
+/* Solver(block_dim=...) override (solver.mojo:63-76): threads per block of the generic kernel
+ * (multiple of 32, 32..256) or 0 for the built-in choice. */
 lbm_status lbm_set_block_threads(lbm_handle* h, int32_t threads);
+
+/* Kernel choice (no counterpart in the reference, which compiles one kernel per layout):
+ * 0 = automatic (default), 1 = the generic kernel (any tile), 2 = the block-per-tile kernel,
+ * which needs 256-cell tiles with power-of-two sides and Q*N < 2^31 (LBM_EUNSUPPORTED
+ * otherwise).  Both produce identical populations. */
+lbm_status lbm_set_kernel_path(lbm_handle* h, int32_t path);
+
+/* The kernel lbm_*_step will use: 1 generic, 2 block-per-tile, -1 for a null handle. */
+int32_t lbm_kernel_path(const lbm_handle* h);
 
 /* ---- the step ---- */
 

@@ -20,7 +20,10 @@ BUILD = PKG / "_build"
 LIB = PKG / "liblbm_gb300.so"
 
 ARCH_FLAGS = ["-gencode", "arch=compute_103a,code=sm_103a"]
-NVCC_FLAGS = ["-std=c++17", "-O3", "-lineinfo", "-Xcompiler", "-fPIC,-O2", "--expt-relaxed-constexpr"]
+# --fmad=false: every multiply and add is rounded separately, in the same order as the float32
+# CPU oracle, which makes the step bit-exact against it (costs about 2 % of step time).
+NVCC_FLAGS = ["-std=c++17", "-O3", "-lineinfo", "--fmad=false", "-Xcompiler", "-fPIC,-O2",
+              "--expt-relaxed-constexpr"]
 
 
 def nvcc() -> str:
@@ -38,8 +41,12 @@ def _deps() -> list[Path]:
     return _sources() + sorted(CSRC.glob("*.cuh")) + [ROOT / "include" / "lbm_gb300.h", Path(__file__)]
 
 
+def _extra_from_env() -> list[str]:
+    return os.environ.get("LBM_NVCC_EXTRA", "").split()
+
+
 def up_to_date() -> bool:
-    if not LIB.exists():
+    if not LIB.exists() or _extra_from_env():
         return False
     t = LIB.stat().st_mtime
     return all(p.stat().st_mtime <= t for p in _deps())
@@ -59,7 +66,7 @@ def build(force: bool = False, verbose: bool = False, extra_flags: list[str] | N
     if not force and up_to_date():
         return LIB
     BUILD.mkdir(exist_ok=True)
-    extra = list(extra_flags or [])
+    extra = list(extra_flags or []) + _extra_from_env()
     srcs = _sources()
     workers = max(1, min(len(srcs), os.cpu_count() or 1))
     with cf.ThreadPoolExecutor(max_workers=workers) as ex:

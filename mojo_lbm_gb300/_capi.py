@@ -56,6 +56,8 @@ SIGNATURES = {
     "lbm_create": (_i32, [_CFG, _GRID, C.POINTER(_vp)]),
     "lbm_destroy": (_i32, [_vp]),
     "lbm_set_block_threads": (_i32, [_vp, _i32]),
+    "lbm_set_kernel_path": (_i32, [_vp, _i32]),
+    "lbm_kernel_path": (_i32, [_vp]),
     "lbm_double_buffer_step": (_i32, [_vp, _vp, _vp, _vp, _vp, _f32, _vp]),
     "lbm_esoteric_pull_step": (_i32, [_vp, _vp, _vp, _vp, _f32, _i32, _vp]),
     "lbm_run": (_i32, [_vp, _vp, _vp, _vp, _vp, _f32, _i64, _i64, _vp]),

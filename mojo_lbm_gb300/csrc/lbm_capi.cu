@@ -16,11 +16,27 @@ namespace lbm {
 StepLaunch get_step_d2q9(int, int, int, int);
 StepLaunch get_step_d3q19(int, int, int, int);
 StepLaunch get_step_d3q27(int, int, int, int);
+StepLaunch get_tile_step_d2q9(int, int, int, int);
+StepLaunch get_tile_step_d3q19(int, int, int, int);
+StepLaunch get_tile_step_d3q27(int, int, int, int);
 }  // namespace lbm
 
 using namespace lbm;
 
 namespace {
+
+// tile_any[t] = 1 if any flag of tile t is not FLUID; one warp per tile.
+__global__ void __launch_bounds__(256) tile_summary_kernel(const uint8_t* __restrict__ flags, uint32_t ntiles,
+                                                           uint32_t T, uint8_t* __restrict__ tile_any) {
+    const uint32_t warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, lane = threadIdx.x & 31;
+    if (warp >= ntiles) return;
+    const uint8_t* p = flags + (size_t)warp * T;
+    uint32_t any = 0;
+    for (uint32_t i = lane; i < T; i += 32) any |= __ldg(p + i);
+    any = __reduce_or_sync(0xffffffffu, any);
+    if (lane == 0) tile_any[warp] = any != 0u;
+}
+
 
 thread_local std::string g_err;
 
@@ -40,7 +56,7 @@ int lattice_q(int id) { return id == LBM_D2Q9 ? 9 : id == LBM_D3Q19 ? 19 : id ==
 int lattice_d(int id) { return id == LBM_D2Q9 ? 2 : (id == LBM_D3Q19 || id == LBM_D3Q27) ? 3 : -1; }
 
 // Graph cache key for lbm_run: buffers, tau bits, parity of the first step, chunk length.
-using GraphKey = std::tuple<const void*, const void*, const void*, const void*, uint32_t, int, int64_t>;
+using GraphKey = std::tuple<const void*, const void*, const void*, const void*, uint32_t, int, int64_t, int>;
 
 }  // namespace
 
@@ -48,7 +64,12 @@ struct lbm_handle {
     lbm_config_t cfg;
     lbm_grid_t grid;
     LayoutDesc lay;
-    StepLaunch step;
+    StepLaunch step;       // generic kernel (any tile)
+    StepLaunch step_tile;  // block-per-tile kernel, or null when the grid does not qualify
+    int path;              // 0 auto, 1 generic only, 2 block-per-tile only
+    uint8_t* tile_any;     // per-tile "has a non-FLUID flag" bytes for the block-per-tile kernel
+    uint32_t ntiles;
+    uint32_t mx, my, shx, shxy;
     int threads;
     int device;
     int sm_count;
@@ -91,7 +112,22 @@ StepArgs step_args(const lbm_handle* h, const void* f_in, void* f_out, float* bc
     a.cap_rho = h->cfg.capture_density;
     a.cap_u = h->cfg.capture_velocity;
     a.even = even;
+    a.tile_any = h->tile_any;
+    a.mx = h->mx;
+    a.my = h->my;
+    a.shx = h->shx;
+    a.shxy = h->shxy;
     return a;
+}
+
+bool use_tile(const lbm_handle* h) { return h->step_tile != nullptr && h->path != 1; }
+
+// Rebuilds the per-tile summary of `flags` for the block-per-tile kernel.
+lbm_status tile_summary(lbm_handle* h, const uint8_t* flags, cudaStream_t s) {
+    const uint32_t blocks = (h->ntiles * 32u + 255u) / 256u;
+    tile_summary_kernel<<<blocks, 256, 0, s>>>(flags, h->ntiles, h->lay.T, h->tile_any);
+    LBM_CK(cudaGetLastError());
+    return LBM_OK;
 }
 
 uint32_t blocks_for(uint32_t n, int threads) { return (n + (uint32_t)threads - 1u) / (uint32_t)threads; }
@@ -101,12 +137,25 @@ lbm_status check_handle(const lbm_handle* h) {
     return LBM_OK;
 }
 
+// One step.  with_summary: rebuild the tile summary from `flags` first (single-step calls; a
+// multi-step run builds it once, since flags cannot change inside the run).
 lbm_status step_once(lbm_handle* h, const void* f_in, void* f_out, float* bc, const uint8_t* flags, float tau,
-                     int even, cudaStream_t s) {
+                     int even, cudaStream_t s, bool with_summary = true) {
     const StepArgs a = step_args(h, f_in, f_out, bc, flags, tau, even);
-    LBM_CK(h->step(a, h->threads, s));
+    if (use_tile(h)) {
+        if (with_summary) {
+            const lbm_status st = tile_summary(h, flags, s);
+            if (st != LBM_OK) return st;
+        }
+        LBM_CK(h->step_tile(a, h->threads, s));
+    } else {
+        LBM_CK(h->step(a, h->threads, s));
+    }
     return LBM_OK;
 }
+
+bool pow2(int v) { return v > 0 && (v & (v - 1)) == 0; }
+int ilog2(int v) { int r = 0; while ((1 << r) < v) ++r; return r; }
 
 template <class F>
 lbm_status dispatch_lattice(int lattice, F&& f) {
@@ -189,6 +238,21 @@ lbm_status lbm_create(const lbm_config_t* cfg, const lbm_grid_t* grid, lbm_handl
     h->step = grid->lattice == LBM_D2Q9 ? get_step_d2q9(m, f16, co, les)
             : grid->lattice == LBM_D3Q19 ? get_step_d3q19(m, f16, co, les)
                                          : get_step_d3q27(m, f16, co, les);
+    // block-per-tile kernel: 256-cell tiles with power-of-two sides and 32-bit offsets
+    const int64_t Q = lattice_q(grid->lattice);
+    const bool tile_ok = (int64_t)grid->tx * grid->ty * grid->tz == (int64_t)kTileCells && pow2(grid->tx) &&
+                         pow2(grid->ty) && pow2(grid->tz) && Q * h->lay.ncells < ((int64_t)1 << 31);
+    h->step_tile = !tile_ok ? nullptr
+                 : grid->lattice == LBM_D2Q9 ? get_tile_step_d2q9(m, f16, co, les)
+                 : grid->lattice == LBM_D3Q19 ? get_tile_step_d3q19(m, f16, co, les)
+                                              : get_tile_step_d3q27(m, f16, co, les);
+    h->path = 0;
+    h->ntiles = h->lay.ncells / h->lay.T;
+    h->mx = (uint32_t)grid->tx - 1u;
+    h->my = (uint32_t)grid->ty - 1u;
+    h->shx = (uint32_t)ilog2(grid->tx);
+    h->shxy = (uint32_t)(ilog2(grid->tx) + ilog2(grid->ty));
+    h->tile_any = nullptr;
     h->threads = 256;
     h->scratch = nullptr;
     h->capture_stream = nullptr;
@@ -196,6 +260,7 @@ lbm_status lbm_create(const lbm_config_t* cfg, const lbm_grid_t* grid, lbm_handl
     if (e == cudaSuccess) e = cudaDeviceGetAttribute(&h->sm_count, cudaDevAttrMultiProcessorCount, h->device);
     if (e == cudaSuccess) e = cudaMalloc(&h->scratch, sizeof(double) * (kReduceBlocks * kReduceWidth + 8));
     if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&h->capture_stream, cudaStreamNonBlocking);
+    if (e == cudaSuccess && h->step_tile) e = cudaMalloc(&h->tile_any, h->ntiles);
     if (e != cudaSuccess) {
         lbm_destroy(h);
         return fail(LBM_ECUDA, std::string("lbm_create: ") + cudaGetErrorString(e));
@@ -208,6 +273,7 @@ lbm_status lbm_destroy(lbm_handle* h) {
     if (!h) return LBM_OK;
     for (auto& kv : h->graphs) cudaGraphExecDestroy(kv.second);
     if (h->scratch) cudaFree(h->scratch);
+    if (h->tile_any) cudaFree(h->tile_any);
     if (h->capture_stream) cudaStreamDestroy(h->capture_stream);
     delete h;
     return LBM_OK;
@@ -221,6 +287,17 @@ lbm_status lbm_set_block_threads(lbm_handle* h, int32_t threads) {
     h->threads = threads;
     return LBM_OK;
 }
+
+lbm_status lbm_set_kernel_path(lbm_handle* h, int32_t path) {
+    if (check_handle(h)) return LBM_EINVAL;
+    if (path < 0 || path > 2) return fail(LBM_EINVAL, "path must be 0 (auto), 1 (generic) or 2 (block-per-tile)");
+    if (path == 2 && !h->step_tile)
+        return fail(LBM_EUNSUPPORTED, "the block-per-tile kernel needs 256-cell power-of-two tiles and Q*N < 2^31");
+    h->path = path;
+    return LBM_OK;
+}
+
+int32_t lbm_kernel_path(const lbm_handle* h) { return h ? (use_tile(h) ? 2 : 1) : -1; }
 
 lbm_status lbm_double_buffer_step(lbm_handle* h, void* f_out, const void* f_in, float* bc, const uint8_t* flags,
                                   float tau, void* stream) {
@@ -257,10 +334,16 @@ lbm_status lbm_run(lbm_handle* h, void* f_a, void* f_b, float* bc, const uint8_t
                 h->cfg.capture_velocity))
         return fail(LBM_EINVAL, "bc is required by this configuration");
     cudaStream_t s = (cudaStream_t)stream;
+    if (n_steps == 0) return LBM_OK;
+    if (use_tile(h)) {
+        const lbm_status st = tile_summary(h, flags, s);
+        if (st != LBM_OK) return st;
+    }
     auto launch_k = [&](int64_t k) -> lbm_status {
         const bool a_is_src = ((first_step + k) % 2) == 0;
-        if (eso) return step_once(h, f_a, f_a, bc, flags, tau, a_is_src ? 1 : 0, s);
-        return a_is_src ? step_once(h, f_a, f_b, bc, flags, tau, 0, s) : step_once(h, f_b, f_a, bc, flags, tau, 0, s);
+        if (eso) return step_once(h, f_a, f_a, bc, flags, tau, a_is_src ? 1 : 0, s, false);
+        return a_is_src ? step_once(h, f_a, f_b, bc, flags, tau, 0, s, false)
+                        : step_once(h, f_b, f_a, bc, flags, tau, 0, s, false);
     };
     // Chunks of an even number of steps keep the buffer/parity pattern of every replay identical.
     const int64_t chunk = 64;
@@ -268,7 +351,7 @@ lbm_status lbm_run(lbm_handle* h, void* f_a, void* f_b, float* bc, const uint8_t
     if (n_steps >= chunk) {
         uint32_t tau_bits;
         std::memcpy(&tau_bits, &tau, 4);
-        const GraphKey key{f_a, f_b, bc, flags, tau_bits, (int)(first_step % 2), chunk};
+        const GraphKey key{f_a, f_b, bc, flags, tau_bits, (int)(first_step % 2), chunk, use_tile(h) ? 2 : 1};
         auto it = h->graphs.find(key);
         if (it == h->graphs.end()) {
             cudaGraph_t g = nullptr;
@@ -279,7 +362,8 @@ lbm_status lbm_run(lbm_handle* h, void* f_a, void* f_b, float* bc, const uint8_t
                 const StepArgs a = eso ? step_args(h, f_a, f_a, bc, flags, tau, a_is_src ? 1 : 0)
                                        : (a_is_src ? step_args(h, f_a, f_b, bc, flags, tau, 0)
                                                    : step_args(h, f_b, f_a, bc, flags, tau, 0));
-                if (h->step(a, h->threads, h->capture_stream) != cudaSuccess) st = LBM_ECUDA;
+                const StepLaunch fn = use_tile(h) ? h->step_tile : h->step;
+                if (fn(a, h->threads, h->capture_stream) != cudaSuccess) st = LBM_ECUDA;
             }
             cudaError_t e = cudaStreamEndCapture(h->capture_stream, &g);
             if (st != LBM_OK || e != cudaSuccess) {

@@ -25,6 +25,9 @@ struct StepArgs {
     const uint8_t* flags;
     float tau, Cs, trt_lambda;
     int32_t ddf, moving, eqbc, cap_rho, cap_u, even;
+    // block-per-tile path (256-cell tiles with power-of-two sides)
+    const uint8_t* tile_any;   // per tile: 1 if any flag of the tile is not FLUID (0)
+    uint32_t mx, my, shx, shxy; // lx = t & mx, ly = (t >> shx) & my, lz = t >> shxy
 };
 
 // Storage traits: float32, or Float16C codes decoded to float32 (load_f / store_f,
@@ -233,6 +236,68 @@ __device__ __forceinline__ void collide(float (&f)[L::Q], float tau, const StepA
     }
 }
 
+// moving_wall_bc (src/lbm/kernels/ops/boundary_condition.mojo:17-83): for pulls from a SOLID
+// (enum) node, f_q += 6 w_q rho_w (c_q . u_w) with u_w, rho_w read at the solid node.
+// bc_base(q) returns the element offset of component 0 of the pull neighbour's bc.
+template <class L, class BcBase>
+__device__ __forceinline__ void moving_wall(float (&f)[L::Q], uint32_t nib_solid, const float* bc, uint32_t T,
+                                            BcBase&& bc_base) {
+    constexpr int Q = L::Q, D = L::D;
+    static_for<1, Q>([&](auto qc) {
+        constexpr int q = qc.value;
+        if ((nib_solid >> q) & 1u) {
+            const uint64_t b = bc_base(qc);
+            float cu = 0.f;
+            static_for<0, D>([&](auto dc) {
+                constexpr int d = dc.value;
+                if constexpr (L::c(q, d) > 0) cu += bc[b + (uint64_t)T * d];
+                else if constexpr (L::c(q, d) < 0) cu -= bc[b + (uint64_t)T * d];
+            });
+            constexpr float six_w = 6.f * wf<L>(q);
+            f[q] += six_w * bc[b + (uint64_t)T * D] * cu;
+        }
+    });
+}
+
+// equilibrium_bc + get_density_and_velocity_for_eq_BC (ops/boundary_condition.mojo:87-205):
+// populations pulled across the domain edge count as their rest value; NaN bc components are
+// free and come from the node itself.
+template <class L>
+__device__ __forceinline__ void equilibrium_bc(float (&f)[L::Q], const float* bc, uint64_t own_bc, uint32_t T,
+                                               int32_t gx, int32_t gy, int32_t gz, const LayoutDesc& lay, bool ddf) {
+    constexpr int Q = L::Q, D = L::D;
+    float ub[3] = {0.f, 0.f, 0.f};
+    static_for<0, D>([&](auto dc) { ub[dc.value] = bc[own_bc + (uint64_t)T * dc.value]; });
+    const float rb = bc[own_bc + (uint64_t)T * D];
+    const int32_t g[3] = {gx, gy, gz}, ng[3] = {lay.nx, lay.ny, lay.nz};
+    float rl = 0.f, ul[3] = {0.f, 0.f, 0.f};
+    static_for<0, Q>([&](auto qc) {
+        constexpr int q = qc.value;
+        bool oob = false;
+        static_for<0, D>([&](auto dc) {
+            constexpr int d = dc.value;
+            const int32_t pi = g[d] - L::c(q, d);
+            oob = oob || pi < 0 || pi >= ng[d];
+        });
+        const float fq = oob ? (ddf ? 0.f : wf<L>(q)) : f[q];
+        rl += fq;
+        static_for<0, D>([&](auto dc) {
+            constexpr int d = dc.value;
+            if constexpr (L::c(q, d) > 0) ul[d] += fq;
+            else if constexpr (L::c(q, d) < 0) ul[d] -= fq;
+        });
+    });
+    if (ddf) rl += 1.f;
+    static_for<0, D>([&](auto dc) { ul[dc.value] = ul[dc.value] / rl; });
+    const bool ufree = isnan(ub[0]);
+    float us[3];
+    static_for<0, D>([&](auto dc) { us[dc.value] = ufree ? ul[dc.value] : ub[dc.value]; });
+    const float rs = isnan(rb) ? rl : rb;
+    float uu = 0.f;
+    static_for<0, D>([&](auto dc) { uu += us[dc.value] * us[dc.value]; });
+    static_for<0, Q>([&](auto qc) { f[qc.value] = feq<L, qc.value>(rs, us, uu, ddf); });
+}
+
 template <class L, int METHOD, bool F16C, int COLL, bool LES>
 __global__ void __launch_bounds__(256) step_kernel(const StepArgs a) {
     using P = Pop<F16C>;
@@ -271,30 +336,16 @@ __global__ void __launch_bounds__(256) step_kernel(const StepArgs a) {
     S* fout = (S*)a.f_out;
     const uint64_t own = loc + TQ * tile;
 
-    // ---- neighbour flags at x - c_q (set_adjacent_flags, ops/load_and_store.mojo:270-291)
-    uint32_t raw_solid = 0u, nib_solid = 0u;
-    const bool need_flags = !ESO || a.moving;
-    if (need_flags) {
-        static_for<1, Q>([&](auto qc) {
-            constexpr int q = qc.value;
-            constexpr int sx = -L::c(q, 0), sy = -L::c(q, 1), sz = -L::c(q, 2);
-            const uint32_t m = nb.template loc<sx, sy, sz>() + T * nb.template til<sx, sy, sz>();
-            const uint8_t pf = __ldg(a.flags + m);
-            if (pf == LBM_FLAG_SOLID) raw_solid |= 1u << q;
-            if ((pf & 0x0F) == LBM_FLAG_SOLID) nib_solid |= 1u << q;
-        });
-    }
-
-    // ---- stream
+    // ---- stream.  The pull loads are issued first and do not wait for the neighbour flags; the
+    // few populations whose pull neighbour is SOLID are re-loaded afterwards from the cell's own
+    // opposite slot (mid-grid bounce-back on a raw SOLID compare, ops/load_and_store.mojo:210-219,
+    // which also loads the pull value first).
     float f[Q];
     if constexpr (!ESO) {
         static_for<0, Q>([&](auto qc) {
             constexpr int q = qc.value;
             constexpr int sx = -L::c(q, 0), sy = -L::c(q, 1), sz = -L::c(q, 2);
-            const uint64_t pull = nb.template loc<sx, sy, sz>() + TQ * nb.template til<sx, sy, sz>() + (uint64_t)T * q;
-            const uint64_t bounce = own + (uint64_t)T * opp<L>(q);
-            // mid-grid bounce-back on a raw SOLID compare (ops/load_and_store.mojo:216)
-            f[q] = P::ld(fin + ((raw_solid >> q) & 1u ? bounce : pull));
+            f[q] = P::ld(fin + nb.template loc<sx, sy, sz>() + TQ * nb.template til<sx, sy, sz>() + (uint64_t)T * q);
         });
     } else {
         const bool ev = a.even != 0;
@@ -309,63 +360,41 @@ __global__ void __launch_bounds__(256) step_kernel(const StepArgs a) {
         });
     }
 
-    // ---- boundary conditions (steps/apply_boundary_condition.mojo:10-41)
-    if (a.moving && nib_solid) {
-        const float* bc = a.bc;
-        const uint64_t TK = (uint64_t)T * K;
+    // ---- neighbour flags at x - c_q (set_adjacent_flags, ops/load_and_store.mojo:270-291)
+    uint32_t raw_solid = 0u, nib_solid = 0u;
+    const bool need_flags = !ESO || a.moving;
+    if (need_flags) {
         static_for<1, Q>([&](auto qc) {
             constexpr int q = qc.value;
-            if ((nib_solid >> q) & 1u) {
-                constexpr int sx = -L::c(q, 0), sy = -L::c(q, 1), sz = -L::c(q, 2);
-                const uint64_t b = nb.template loc<sx, sy, sz>() + TK * nb.template til<sx, sy, sz>();
-                float cu = 0.f;
-                static_for<0, D>([&](auto dc) {
-                    constexpr int d = dc.value;
-                    if constexpr (L::c(q, d) > 0) cu += bc[b + (uint64_t)T * d];
-                    else if constexpr (L::c(q, d) < 0) cu -= bc[b + (uint64_t)T * d];
-                });
-                constexpr float six_w = 6.f * wf<L>(q);
-                f[q] += six_w * bc[b + (uint64_t)T * D] * cu;
-            }
+            constexpr int sx = -L::c(q, 0), sy = -L::c(q, 1), sz = -L::c(q, 2);
+            const uint32_t m = nb.template loc<sx, sy, sz>() + T * nb.template til<sx, sy, sz>();
+            const uint8_t pf = __ldg(a.flags + m);
+            if (pf == LBM_FLAG_SOLID) raw_solid |= 1u << q;
+            if ((pf & 0x0F) == LBM_FLAG_SOLID) nib_solid |= 1u << q;
+        });
+    }
+    if constexpr (!ESO) {
+        if (raw_solid) {
+            static_for<1, Q>([&](auto qc) {
+                constexpr int q = qc.value;
+                if ((raw_solid >> q) & 1u) f[q] = P::ld(fin + own + (uint64_t)T * opp<L>(q));
+            });
+        }
+    }
+
+    // ---- boundary conditions (steps/apply_boundary_condition.mojo:10-41)
+    if (a.moving && nib_solid) {
+        const uint64_t TK = (uint64_t)T * K;
+        moving_wall<L>(f, nib_solid, a.bc, T, [&](auto qc) -> uint64_t {
+            constexpr int q = decltype(qc)::value;
+            constexpr int sx = -L::c(q, 0), sy = -L::c(q, 1), sz = -L::c(q, 2);
+            return nb.template loc<sx, sy, sz>() + TK * nb.template til<sx, sy, sz>();
         });
     }
     const uint64_t own_bc = loc + (uint64_t)T * K * tile;
-    if (a.eqbc && (flag & 0x0F) == LBM_FLAG_EQUILIBRIUM) {
-        const bool ddf = a.ddf != 0;
-        const float* bc = a.bc;
-        float ub[3] = {0.f, 0.f, 0.f};
-        static_for<0, D>([&](auto dc) { ub[dc.value] = bc[own_bc + (uint64_t)T * dc.value]; });
-        const float rb = bc[own_bc + (uint64_t)T * D];
-        const int32_t gx = (int32_t)(bx * a.lay.tx + lx), gy = (int32_t)(by * a.lay.ty + ly),
-                      gz = (int32_t)(bz * a.lay.tz + lz);
-        const int32_t g[3] = {gx, gy, gz}, ng[3] = {a.lay.nx, a.lay.ny, a.lay.nz};
-        float rl = 0.f, ul[3] = {0.f, 0.f, 0.f};
-        static_for<0, Q>([&](auto qc) {
-            constexpr int q = qc.value;
-            bool oob = false;
-            static_for<0, D>([&](auto dc) {
-                constexpr int d = dc.value;
-                const int32_t pi = g[d] - L::c(q, d);
-                oob = oob || pi < 0 || pi >= ng[d];
-            });
-            const float fq = oob ? (ddf ? 0.f : wf<L>(q)) : f[q];
-            rl += fq;
-            static_for<0, D>([&](auto dc) {
-                constexpr int d = dc.value;
-                if constexpr (L::c(q, d) > 0) ul[d] += fq;
-                else if constexpr (L::c(q, d) < 0) ul[d] -= fq;
-            });
-        });
-        if (ddf) rl += 1.f;
-        static_for<0, D>([&](auto dc) { ul[dc.value] = ul[dc.value] / rl; });
-        const bool ufree = isnan(ub[0]);
-        float us[3];
-        static_for<0, D>([&](auto dc) { us[dc.value] = ufree ? ul[dc.value] : ub[dc.value]; });
-        const float rs = isnan(rb) ? rl : rb;
-        float uu = 0.f;
-        static_for<0, D>([&](auto dc) { uu += us[dc.value] * us[dc.value]; });
-        static_for<0, Q>([&](auto qc) { f[qc.value] = feq<L, qc.value>(rs, us, uu, ddf); });
-    }
+    if (a.eqbc && (flag & 0x0F) == LBM_FLAG_EQUILIBRIUM)
+        equilibrium_bc<L>(f, a.bc, own_bc, T, (int32_t)(bx * a.lay.tx + lx), (int32_t)(by * a.lay.ty + ly),
+                          (int32_t)(bz * a.lay.tz + lz), a.lay, a.ddf != 0);
 
     collide<L, COLL, LES>(f, a.tau, a, a.bc + own_bc, T, flag);
 
@@ -387,6 +416,166 @@ __global__ void __launch_bounds__(256) step_kernel(const StepArgs a) {
     }
 }
 
+// ---------------------------------------------------------------------------------------------
+// Block-per-tile path.  One CTA of 256 threads is one 256-cell tile with power-of-two sides, so
+// the in-tile coordinates are shifts of threadIdx, the tile coordinates are block-uniform, the
+// population offsets q*T are immediates and every neighbour offset is the own offset plus three
+// per-axis deltas computed once per thread (32-bit: requires Q*N < 2^31).  Before touching any
+// flag, a warp checks the tile-summary bytes of its tile and the 26 neighbouring tiles: when all
+// are zero every cell it owns is FLUID with FLUID neighbours, so the neighbour-flag gather and
+// every boundary branch are skipped (the common case away from walls).  Results are identical
+// to step_kernel.
+// ---------------------------------------------------------------------------------------------
+constexpr uint32_t kTileCells = 256;
+
+template <class L, int METHOD, bool F16C, int COLL, bool LES>
+__global__ void __launch_bounds__(256, (COLL == LBM_KBC) ? 2 : (L::Q == 27 ? 3 : 4)) step_kernel_tile(const StepArgs a) {
+    using P = Pop<F16C>;
+    using S = typename P::T;
+    constexpr int Q = L::Q, D = L::D, K = D + 1;
+    constexpr uint32_t T = kTileCells;
+    constexpr bool ESO = METHOD == LBM_ESOTERIC_PULL;
+
+    const uint32_t tile = blockIdx.x, tid = threadIdx.x;
+    const uint32_t n = tid + T * tile;  // cell index = flag offset
+    const uint32_t byz = a.lay.d_ntx.div(tile);
+    const uint32_t bx = tile - byz * (uint32_t)a.lay.ntx;
+    const uint32_t bz = a.lay.d_nty.div(byz);
+    const uint32_t by = byz - bz * (uint32_t)a.lay.nty;
+    const int32_t ntx = a.lay.ntx, nty = a.lay.nty, ntz = a.lay.ntz;
+
+    // ---- is this warp's neighbourhood all FLUID?  (lanes 0..26: the 3x3x3 tile block)
+    const uint32_t lane = tid & 31u;
+    uint32_t special = 0u;
+    if (lane < 27u) {
+        const int32_t ox = (int32_t)(lane % 3u) - 1, oy = (int32_t)((lane / 3u) % 3u) - 1, oz = (int32_t)(lane / 9u) - 1;
+        int32_t tx_ = (int32_t)bx + ox, ty_ = (int32_t)by + oy, tz_ = (int32_t)bz + oz;
+        tx_ = tx_ < 0 ? tx_ + ntx : (tx_ >= ntx ? tx_ - ntx : tx_);
+        ty_ = ty_ < 0 ? ty_ + nty : (ty_ >= nty ? ty_ - nty : ty_);
+        tz_ = tz_ < 0 ? tz_ + ntz : (tz_ >= ntz ? tz_ - ntz : tz_);
+        special = __ldg(a.tile_any + (tx_ + ntx * (ty_ + nty * tz_)));
+    }
+    const bool clean = __ballot_sync(0xffffffffu, special != 0u) == 0u;
+
+    uint8_t flag = 0;
+    if (!clean) {
+        flag = __ldg(a.flags + n);
+        // is_valid_thread (src/lbm/kernels/utils/checks.mojo:55-60)
+        if ((flag & 0x0F) == LBM_FLAG_SOLID || (flag & LBM_FLAG_EXCLUDE)) return;
+    }
+
+    // ---- per-axis neighbour deltas, in cells (flags, bc) and in population elements (f)
+    const int32_t tx = a.lay.tx, ty = a.lay.ty, tz = a.lay.tz, txy = tx * ty;
+    const uint32_t lx = tid & a.mx, ly = (tid >> a.shx) & a.my, lz = tid >> a.shxy;
+    const int32_t TQ = (int32_t)(T * Q);
+    int32_t dc[3][3], dp[3][3];
+    {
+        const int32_t jxm = bx > 0 ? -1 : ntx - 1, jxp = (int32_t)bx + 1 < ntx ? 1 : 1 - ntx;
+        const int32_t jym = by > 0 ? -ntx : (nty - 1) * ntx, jyp = (int32_t)by + 1 < nty ? ntx : (1 - nty) * ntx;
+        dc[0][1] = dp[0][1] = dc[1][1] = dp[1][1] = dc[2][1] = dp[2][1] = 0;
+        if (lx > 0) dc[0][0] = dp[0][0] = -1;
+        else { dc[0][0] = (tx - 1) + (int32_t)T * jxm; dp[0][0] = (tx - 1) + TQ * jxm; }
+        if ((int32_t)lx + 1 < tx) dc[0][2] = dp[0][2] = 1;
+        else { dc[0][2] = (1 - tx) + (int32_t)T * jxp; dp[0][2] = (1 - tx) + TQ * jxp; }
+        if (ly > 0) dc[1][0] = dp[1][0] = -tx;
+        else { dc[1][0] = (ty - 1) * tx + (int32_t)T * jym; dp[1][0] = (ty - 1) * tx + TQ * jym; }
+        if ((int32_t)ly + 1 < ty) dc[1][2] = dp[1][2] = tx;
+        else { dc[1][2] = (1 - ty) * tx + (int32_t)T * jyp; dp[1][2] = (1 - ty) * tx + TQ * jyp; }
+        if constexpr (D == 3) {
+            const int32_t ntxy = ntx * nty;
+            const int32_t jzm = bz > 0 ? -ntxy : (ntz - 1) * ntxy, jzp = (int32_t)bz + 1 < ntz ? ntxy : (1 - ntz) * ntxy;
+            if (lz > 0) dc[2][0] = dp[2][0] = -txy;
+            else { dc[2][0] = (tz - 1) * txy + (int32_t)T * jzm; dp[2][0] = (tz - 1) * txy + TQ * jzm; }
+            if ((int32_t)lz + 1 < tz) dc[2][2] = dp[2][2] = txy;
+            else { dc[2][2] = (1 - tz) * txy + (int32_t)T * jzp; dp[2][2] = (1 - tz) * txy + TQ * jzp; }
+        } else {
+            dc[2][0] = dc[2][2] = dp[2][0] = dp[2][2] = 0;
+        }
+    }
+    const int32_t own = (int32_t)tid + TQ * (int32_t)tile;
+    const S* fin = (const S*)a.f_in;
+    S* fout = (S*)a.f_out;
+
+    // ---- stream (pull loads first, independent of the flags)
+    float f[Q];
+    if constexpr (!ESO) {
+        static_for<0, Q>([&](auto qc) {
+            constexpr int q = qc.value;
+            constexpr int sx = -L::c(q, 0), sy = -L::c(q, 1), sz = -L::c(q, 2);
+            const int32_t o = own + dp[0][sx + 1] + dp[1][sy + 1] + dp[2][sz + 1];
+            f[q] = P::ld(fin + o + (int32_t)(T * q));
+        });
+    } else {
+        // even: pos from (x, pos), neg from (x + c_pos, neg); odd: pos from (x, neg), neg from
+        // (x + c_pos, pos).  Slot pos + 1 = neg, so the parity folds into two base pointers.
+        const bool ev = a.even != 0;
+        const S* finA = fin + (ev ? 0u : T);
+        const S* finB = fin + (ev ? T : 0u);
+        f[0] = P::ld_rw(fin + own);
+        static_for<1, Q - 1, 2>([&](auto qc) {
+            constexpr int pos = qc.value, neg = pos + 1;
+            constexpr int sx = L::c(pos, 0), sy = L::c(pos, 1), sz = L::c(pos, 2);
+            const int32_t o = own + dp[0][sx + 1] + dp[1][sy + 1] + dp[2][sz + 1];
+            f[pos] = P::ld_rw(finA + own + (int32_t)(T * pos));
+            f[neg] = P::ld_rw(finB + o + (int32_t)(T * pos));
+        });
+    }
+
+    if (!clean) {
+        // ---- neighbour flags at x - c_q (set_adjacent_flags, ops/load_and_store.mojo:270-291)
+        uint32_t raw_solid = 0u, nib_solid = 0u;
+        if (!ESO || a.moving) {
+            static_for<1, Q>([&](auto qc) {
+                constexpr int q = qc.value;
+                constexpr int sx = -L::c(q, 0), sy = -L::c(q, 1), sz = -L::c(q, 2);
+                const uint8_t pf = __ldg(a.flags + ((int32_t)n + dc[0][sx + 1] + dc[1][sy + 1] + dc[2][sz + 1]));
+                if (pf == LBM_FLAG_SOLID) raw_solid |= 1u << q;
+                if ((pf & 0x0F) == LBM_FLAG_SOLID) nib_solid |= 1u << q;
+            });
+        }
+        if constexpr (!ESO) {
+            // mid-grid bounce-back on a raw SOLID compare (ops/load_and_store.mojo:216)
+            if (raw_solid)
+                static_for<1, Q>([&](auto qc) {
+                    constexpr int q = qc.value;
+                    if ((raw_solid >> q) & 1u) f[q] = P::ld(fin + own + (int32_t)(T * opp<L>(q)));
+                });
+        }
+        if (a.moving && nib_solid) {
+            moving_wall<L>(f, nib_solid, a.bc, T, [&](auto qc) -> uint64_t {
+                constexpr int q = decltype(qc)::value;
+                constexpr int sx = -L::c(q, 0), sy = -L::c(q, 1), sz = -L::c(q, 2);
+                const uint32_t m = (uint32_t)((int32_t)n + dc[0][sx + 1] + dc[1][sy + 1] + dc[2][sz + 1]);
+                const uint32_t mt = m / T;
+                return (uint64_t)(m - mt * T) + (uint64_t)T * K * mt;
+            });
+        }
+        if (a.eqbc && (flag & 0x0F) == LBM_FLAG_EQUILIBRIUM)
+            equilibrium_bc<L>(f, a.bc, tid + (uint64_t)T * K * tile, T, (int32_t)(bx * tx + lx),
+                              (int32_t)(by * ty + ly), (int32_t)(bz * tz + lz), a.lay, a.ddf != 0);
+    }
+
+    collide<L, COLL, LES>(f, a.tau, a, a.bc + (tid + (uint64_t)T * K * tile), T, flag);
+
+    // ---- store
+    if constexpr (!ESO) {
+        S* po = fout + own;
+        static_for<0, Q>([&](auto qc) { P::st(po + (int32_t)(T * qc.value), f[qc.value]); });
+    } else {
+        const bool ev = a.even != 0;
+        S* foA = fout + (ev ? 0u : T);
+        S* foB = fout + (ev ? T : 0u);
+        P::st(fout + own, f[0]);
+        static_for<1, Q - 1, 2>([&](auto qc) {
+            constexpr int pos = qc.value, neg = pos + 1;
+            constexpr int sx = L::c(pos, 0), sy = L::c(pos, 1), sz = L::c(pos, 2);
+            const int32_t o = own + dp[0][sx + 1] + dp[1][sy + 1] + dp[2][sz + 1];
+            P::st(foB + o + (int32_t)(T * pos), f[pos]);
+            P::st(foA + own + (int32_t)(T * pos), f[neg]);
+        });
+    }
+}
+
 // Launcher type used by the dispatch tables.
 using StepLaunch = cudaError_t (*)(const StepArgs&, int threads, cudaStream_t);
 
@@ -397,23 +586,21 @@ cudaError_t launch_step(const StepArgs& a, int threads, cudaStream_t s) {
     return cudaGetLastError();
 }
 
-// Table of the 32 variants of one lattice, indexed by
-// ((method*2 + f16c)*4 + collision)*2 + les.
-template <class L>
-struct StepTable {
-    static StepLaunch get(int method, int f16c, int coll, int les) {
-        static const StepLaunch t[32] = {
-#define LBM_ROW(M, F)                                                                         \
-    &launch_step<L, M, F, LBM_SRT, false>, &launch_step<L, M, F, LBM_SRT, true>,              \
-        &launch_step<L, M, F, LBM_TRT, false>, &launch_step<L, M, F, LBM_TRT, true>,          \
-        &launch_step<L, M, F, LBM_KBC, false>, &launch_step<L, M, F, LBM_KBC, true>,          \
-        &launch_step<L, M, F, LBM_RLBM, false>, &launch_step<L, M, F, LBM_RLBM, true>
-            LBM_ROW(LBM_DOUBLE_BUFFER, false), LBM_ROW(LBM_DOUBLE_BUFFER, true),
-            LBM_ROW(LBM_ESOTERIC_PULL, false), LBM_ROW(LBM_ESOTERIC_PULL, true)
-#undef LBM_ROW
-        };
-        return t[((method * 2 + f16c) * 4 + coll) * 2 + les];
-    }
-};
+template <class L, int METHOD, bool F16C, int COLL, bool LES>
+cudaError_t launch_step_tile(const StepArgs& a, int, cudaStream_t s) {
+    step_kernel_tile<L, METHOD, F16C, COLL, LES><<<a.lay.ncells / kTileCells, kTileCells, 0, s>>>(a);
+    return cudaGetLastError();
+}
+
+// Tables of the 32 variants of one lattice, indexed by ((method*2 + f16c)*4 + collision)*2 + les.
+#define LBM_STEP_ROW(FN, L, M, F)                                                              \
+    &FN<L, M, F, LBM_SRT, false>, &FN<L, M, F, LBM_SRT, true>, &FN<L, M, F, LBM_TRT, false>,   \
+        &FN<L, M, F, LBM_TRT, true>, &FN<L, M, F, LBM_KBC, false>, &FN<L, M, F, LBM_KBC, true>, \
+        &FN<L, M, F, LBM_RLBM, false>, &FN<L, M, F, LBM_RLBM, true>
+#define LBM_STEP_TABLE(FN, L)                                                                  \
+    {LBM_STEP_ROW(FN, L, LBM_DOUBLE_BUFFER, false), LBM_STEP_ROW(FN, L, LBM_DOUBLE_BUFFER, true), \
+     LBM_STEP_ROW(FN, L, LBM_ESOTERIC_PULL, false), LBM_STEP_ROW(FN, L, LBM_ESOTERIC_PULL, true)}
+
+inline int step_index(int method, int f16c, int coll, int les) { return ((method * 2 + f16c) * 4 + coll) * 2 + les; }
 
 }  // namespace lbm

@@ -1,8 +1,9 @@
-// The 32 fused-step variants of the D3Q19 lattice (get_D3Q19, src/lbm/lattice.mojo:221-299).
+// The 32 generic fused-step variants of the D3Q19 lattice (any tile shape, 64-bit offsets).
 #include "lbm_step.cuh"
 
 namespace lbm {
 StepLaunch get_step_d3q19(int method, int f16c, int coll, int les) {
-    return StepTable<D3Q19>::get(method, f16c, coll, les);
+    static const StepLaunch t[32] = LBM_STEP_TABLE(launch_step, D3Q19);
+    return t[step_index(method, f16c, coll, les)];
 }
 }  // namespace lbm

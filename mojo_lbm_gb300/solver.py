@@ -43,6 +43,14 @@ class Solver:
     def set_block_threads(self, threads: int) -> None:
         check(self._lib.lbm_set_block_threads(self._h, int(threads)))
 
+    def set_kernel_path(self, path: int) -> None:
+        """0 automatic, 1 generic kernel, 2 block-per-tile kernel (identical results)."""
+        check(self._lib.lbm_set_kernel_path(self._h, int(path)))
+
+    @property
+    def kernel_path(self) -> int:
+        return int(self._lib.lbm_kernel_path(self._h))
+
     # -- the step (solver.mojo:81-154) ------------------------------------------------------
     def double_buffer_step(self, f_out, f_in, bc, flags, tau: float, stream=None) -> None:
         check(self._lib.lbm_double_buffer_step(self._h, ptr(f_out), ptr(f_in), ptr(bc), ptr(flags), float(tau),
