@@ -183,6 +183,19 @@ lbm_status lbm_compute_rho_u(lbm_handle* h, float* rho, float* u, const void* f,
 lbm_status lbm_reduce_mass_momentum(lbm_handle* h, const void* f, const uint8_t* flags,
                                     int32_t after_odd_step, double out[4], void* stream);
 
+/* No counterpart in the reference.  The mass/momentum reduction above for callers that cannot
+ * allocate device memory (an application-owned pool is their only allowed source, or the call
+ * sits where cudaMalloc/cudaFree must not run): it needs no handle and allocates nothing.  Its
+ * scratch is a fixed 1 MiB device array in the library, held by every GPU that loads it until the
+ * process exits, so grids above 2^27 cells (512^3) are rejected with LBM_EINVAL.  The first call
+ * on a device looks that array up (cudaGetSymbolAddress); make it before any stream capture.
+ * Calls share the array: calls that overlap on the GPU (other streams, other threads) race.
+ * Same arguments and results as lbm_reduce_mass_momentum, with (cfg, grid) in place of a handle;
+ * synchronises the stream. */
+lbm_status lbm_reduce_mass_momentum_noalloc(const lbm_config_t* cfg, const lbm_grid_t* grid,
+                                            const void* f, const uint8_t* flags,
+                                            int32_t after_odd_step, double out[4], void* stream);
+
 /* linkwise_bounceback_kernel (geometry/interpolated_BB.mojo:46-141) as launched by
  * RigidStationaryObject.bounceback (geometry/rigidstationary.mojo:127-153): per link, in place
  * on the lattice the last double-buffer step wrote.  fluid_ids are linear flag-layout indices,

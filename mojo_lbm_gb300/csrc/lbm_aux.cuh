@@ -356,7 +356,7 @@ __global__ void __launch_bounds__(kReduceThreads) final_sum_kernel(const double*
 }
 
 // Column sums of an n x D float array (link fastest), partials of width 4.
-__global__ void __launch_bounds__(kReduceThreads) colsum_partial_kernel(const float* v, int64_t n, int D,
+static __global__ void __launch_bounds__(kReduceThreads) colsum_partial_kernel(const float* v, int64_t n, int D,
                                                                         double* partial) {
     double acc[4] = {0.0, 0.0, 0.0, 0.0};
     for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {

@@ -60,6 +60,11 @@ using GraphKey = std::tuple<const void*, const void*, const void*, const void*, 
 
 }  // namespace
 
+namespace lbm {
+// Sets the message lbm_last_error() returns, for entry points defined in other files.
+__attribute__((visibility("hidden"))) void set_last_error(const char* msg) { g_err = msg; }
+}  // namespace lbm
+
 struct lbm_handle {
     lbm_config_t cfg;
     lbm_grid_t grid;
