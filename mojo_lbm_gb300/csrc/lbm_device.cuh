@@ -109,27 +109,34 @@ LBM_HD float as_f32(uint32_t u) {
 #endif
 }
 
+// Decode.  A code with a non-zero exponent field is a normal float32 whose exponent is 112 larger:
+// shifting the 15 magnitude bits up by 12 and adding 112 << 23 produces it.  A code with a zero
+// exponent field (denormal) is M * 2^-25 for its 11-bit mantissa M, exact in float32; this is
+// the value the reference's renormalisation builds bit by bit.
 LBM_HD float f16c_decode(uint32_t h) {
-    const uint32_t e = (h & 0x7800u) >> 11;
-    const uint32_t m = (h & 0x07FFu) << 12;
-    uint32_t r = (h & 0x8000u) << 16;
-    if (e != 0u) r |= ((e + 112u) << 23) | m;
-    else if (m != 0u) {
-        const uint32_t v = as_u32((float)m) >> 23;  // biased exponent of float(m)
-        r |= ((v - 37u) << 23) | ((m << (150u - v)) & 0x007FF000u);
-    }
-    return as_f32(r);
+    const uint32_t mag = h & 0x7FFFu;
+    const uint32_t nrm = (mag << 12) + 0x38000000u;
+    const uint32_t den = as_u32((float)mag * 0x1p-25f);
+    return as_f32(((h & 0x8000u) << 16) | (mag >= 0x0800u ? nrm : den));
 }
 
+// Encode, with the reference's rounding: add 0x800 to the float32 bits (round half up on the
+// first dropped bit), then take the exponent e of the sum:
+//   e > 112       normal code ((e - 112) << 11) | (m >> 12), i.e. (|b| >> 12) - (112 << 11),
+//                 saturated to 0x7FFF when e > 127;
+//   100 < e < 113 denormal code (((0x7FF800 + m) >> (124 - e)) + 1) >> 1;
+//   e < 101       zero.
+// The sign bit is taken from the sum.  Only the low 16 bits are kept.
 LBM_HD uint32_t f16c_encode(float x) {
     const uint32_t b = as_u32(x) + 0x00000800u;
-    const uint32_t e = (b & 0x7F800000u) >> 23;
+    const uint32_t e = (b >> 23) & 0xFFu;
     const uint32_t m = b & 0x007FFFFFu;
-    uint32_t r = (b & 0x80000000u) >> 16;
-    if (e > 112u) r |= (((e - 112u) << 11) & 0x7800u) | (m >> 12);
-    else if (e > 100u) r |= (((0x007FF800u + m) >> (124u - e)) + 1u) >> 1;
-    if (e > 127u) r |= 0x7FFFu;
-    return r & 0xFFFFu;
+    const uint32_t nrm_raw = ((b & 0x7FFFFFFFu) >> 12) - 0x38000u;
+    const uint32_t nrm = nrm_raw < 0x7FFFu ? nrm_raw : 0x7FFFu;
+    const uint32_t sh = e > 112u ? 12u : (e < 101u ? 23u : 124u - e);
+    const uint32_t den = (((0x007FF800u + m) >> sh) + 1u) >> 1;
+    const uint32_t mag = e > 112u ? nrm : (e > 100u ? den : 0u);
+    return ((b & 0x80000000u) >> 16) | mag;
 }
 
 // ---------------------------------------------------------------------------------------------

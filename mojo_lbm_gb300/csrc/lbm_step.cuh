@@ -90,6 +90,47 @@ __device__ __forceinline__ float feq(float rho, const float* u, float uu, bool d
     return w * rho * (1.f + 3.f * eu + 4.5f * eu * eu - 1.5f * uu);
 }
 
+// Visits f_eq of every direction in order q = 0..Q-1, computing each opposite pair (q, q+1) from
+// one dot product: e_{q+1}.u is exactly -(e_q.u) (IEEE sums are sign-symmetric), so 3 e.u and
+// 4.5 (e.u)^2 of the pair follow exactly from those of q, and every value equals feq<L, q>.
+// fn(qc, feq_with_ddf) is called; with BOTH, fn(qc, feq_with_ddf, feq_unshifted).
+template <class L, bool DDF, bool BOTH, class F>
+__device__ __forceinline__ void feq_visit(float rho, const float* u, float uu, F&& fn) {
+    constexpr int Q = L::Q;
+    const float c15 = 1.5f * uu;
+    auto emit = [&](auto qc, float wr, float wm, float t3, float t45) {
+        const float plain = (!DDF || BOTH) ? wr * (((1.f + t3) + t45) - c15) : 0.f;
+        if constexpr (DDF) {
+            const float shifted = wr * ((t3 + t45) - c15) + wm;
+            if constexpr (BOTH) fn(qc, shifted, plain);
+            else fn(qc, shifted);
+        } else {
+            if constexpr (BOTH) fn(qc, plain, plain);
+            else fn(qc, plain);
+        }
+    };
+    {
+        constexpr float w0 = wf<L>(0);
+        emit(std::integral_constant<int, 0>{}, w0 * rho, w0 * (rho - 1.f), 0.f, 0.f);
+    }
+    static_for<1, Q, 2>([&](auto qc) {
+        constexpr int q = qc.value;
+        constexpr float w = wf<L>(q);
+        const float eu = edot<L>(u, q);
+        const float t3 = 3.f * eu;
+        const float t45 = 4.5f * eu * eu;
+        const float wr = w * rho, wm = w * (rho - 1.f);
+        emit(qc, wr, wm, t3, t45);
+        emit(std::integral_constant<int, q + 1>{}, wr, wm, -t3, t45);
+    });
+}
+
+template <class L, bool BOTH = false, class F>
+__device__ __forceinline__ void for_each_feq(float rho, const float* u, float uu, bool ddf, F&& fn) {
+    if (ddf) feq_visit<L, true, BOTH>(rho, u, uu, fn);
+    else feq_visit<L, false, BOTH>(rho, u, uu, fn);
+}
+
 // KBC shear part of the deviatoric non-equilibrium stress.  D2Q9 is get_shear_D2Q9
 // (src/lbm/kernels/ops/collisions/KBC_.mojo:137-175); the 3D form is the same projection for
 // D3Q19/D3Q27 (Karlin, Bösch, Chikatamarla, PRE 90, 031302, 2014).
@@ -152,9 +193,9 @@ __device__ __forceinline__ void collide(float (&f)[L::Q], float tau, const StepA
         // get_non_eq_second_order_moment (src/lbm/kernels/utils/moment.mojo:111-150)
         float P[L::NS];
         static_for<0, L::NS>([&](auto nc) { P[nc.value] = 0.f; });
-        static_for<0, Q>([&](auto qc) {
-            constexpr int q = qc.value;
-            const float fn = f[q] - feq<L, q>(rho, u, uu, ddf);
+        for_each_feq<L>(rho, u, uu, ddf, [&](auto qc, float e) {
+            constexpr int q = decltype(qc)::value;
+            const float fn = f[q] - e;
             static_for<0, L::NS>([&](auto nc) {
                 constexpr int n = nc.value;
                 constexpr int cc = L::c(q, sa<L>(n)) * L::c(q, sb<L>(n));
@@ -178,8 +219,8 @@ __device__ __forceinline__ void collide(float (&f)[L::Q], float tau, const StepA
         if constexpr (COLL == LBM_RLBM) {
             // RLBM (src/lbm/kernels/ops/collisions/collision.mojo:168-223)
             const float one_m = 1.f - 1.f / tau_local;
-            static_for<0, Q>([&](auto qc) {
-                constexpr int q = qc.value;
+            for_each_feq<L>(rho, u, uu, ddf, [&](auto qc, float e) {
+                constexpr int q = decltype(qc)::value;
                 float dot = 0.f;
                 static_for<0, L::NS>([&](auto nc) {
                     constexpr int n = nc.value, A = sa<L>(n), B = sb<L>(n);
@@ -188,26 +229,25 @@ __device__ __forceinline__ void collide(float (&f)[L::Q], float tau, const StepA
                     if constexpr (Qn != 0.f) dot += Qn * P[n];
                 });
                 constexpr float k = (float)(L::wd(q) / (2.0 / 9.0));
-                f[q] = feq<L, q>(rho, u, uu, ddf) + one_m * (k * dot);
+                f[q] = e + one_m * (k * dot);
             });
         } else if constexpr (COLL == LBM_KBC) {
             // KBC (src/lbm/kernels/ops/collisions/KBC_.mojo:180-238); gamma is not clamped
             const float beta = 1.f / (2.f * tau_local);
             const float inv_beta = 2.f * tau_local;
             float sp1 = 0.f, sp2 = 0.f;
-            static_for<0, Q>([&](auto qc) {
-                constexpr int q = qc.value;
-                const float fe0 = feq<L, q>(rho, u, uu, false);
+            for_each_feq<L, true>(rho, u, uu, ddf, [&](auto qc, float e, float fe0) {
+                constexpr int q = decltype(qc)::value;
                 const float ds = kbc_shear<L, q>(P);
-                const float dh = (f[q] - feq<L, q>(rho, u, uu, ddf)) - ds;
+                const float dh = (f[q] - e) - ds;
                 sp1 += ds * dh / fe0;
                 sp2 += dh * dh / fe0;
             });
             const float gamma = inv_beta - (2.f - inv_beta) * sp1 / (sp2 + 1e-32f);
-            static_for<0, Q>([&](auto qc) {
-                constexpr int q = qc.value;
+            for_each_feq<L>(rho, u, uu, ddf, [&](auto qc, float e) {
+                constexpr int q = decltype(qc)::value;
                 const float ds = kbc_shear<L, q>(P);
-                const float dh = (f[q] - feq<L, q>(rho, u, uu, ddf)) - ds;
+                const float dh = (f[q] - e) - ds;
                 f[q] -= beta * (2.f * ds + gamma * dh);
             });
         }
@@ -215,19 +255,21 @@ __device__ __forceinline__ void collide(float (&f)[L::Q], float tau, const StepA
     if constexpr (COLL == LBM_SRT) {
         // SRT (src/lbm/kernels/ops/collisions/collision.mojo:12-46)
         const float inv_tau = 1.f / tau_local;
-        static_for<0, Q>([&](auto qc) {
-            constexpr int q = qc.value;
-            f[q] -= inv_tau * (f[q] - feq<L, q>(rho, u, uu, ddf));
+        for_each_feq<L>(rho, u, uu, ddf, [&](auto qc, float e) {
+            constexpr int q = decltype(qc)::value;
+            f[q] -= inv_tau * (f[q] - e);
         });
     } else if constexpr (COLL == LBM_TRT) {
         // TRT (collision.mojo:49-113) with tau_asymm of steps/collide.mojo:214-215
         const float tau_a = 0.5f + a.trt_lambda / (tau_local - 0.5f);
         const float is = 1.f / tau_local, ia = 1.f / tau_a;
-        f[0] -= is * (f[0] - feq<L, 0>(rho, u, uu, ddf));
+        float eqv[Q];
+        for_each_feq<L>(rho, u, uu, ddf, [&](auto qc, float e) { eqv[decltype(qc)::value] = e; });
+        f[0] -= is * (f[0] - eqv[0]);
         static_for<1, Q, 2>([&](auto qc) {
             constexpr int q = qc.value, o = q + 1;
             const float fs = (f[q] + f[o]) * 0.5f, fa = (f[q] - f[o]) * 0.5f;
-            const float eq = feq<L, q>(rho, u, uu, ddf), eo = feq<L, o>(rho, u, uu, ddf);
+            const float eq = eqv[q], eo = eqv[o];
             const float es = (eq + eo) * 0.5f, ea = (eq - eo) * 0.5f;
             const float sym = is * (fs - es);
             f[q] -= (sym + ia * (fa - ea));
@@ -295,7 +337,7 @@ __device__ __forceinline__ void equilibrium_bc(float (&f)[L::Q], const float* bc
     const float rs = isnan(rb) ? rl : rb;
     float uu = 0.f;
     static_for<0, D>([&](auto dc) { uu += us[dc.value] * us[dc.value]; });
-    static_for<0, Q>([&](auto qc) { f[qc.value] = feq<L, qc.value>(rs, us, uu, ddf); });
+    for_each_feq<L>(rs, us, uu, ddf, [&](auto qc, float e) { f[decltype(qc)::value] = e; });
 }
 
 template <class L, int METHOD, bool F16C, int COLL, bool LES>
@@ -429,7 +471,7 @@ __global__ void __launch_bounds__(256) step_kernel(const StepArgs a) {
 constexpr uint32_t kTileCells = 256;
 
 template <class L, int METHOD, bool F16C, int COLL, bool LES>
-__global__ void __launch_bounds__(256, (COLL == LBM_KBC) ? 2 : (L::Q == 27 ? 3 : 4)) step_kernel_tile(const StepArgs a) {
+__global__ void __launch_bounds__(256, (COLL == LBM_KBC || L::Q == 27) ? 3 : 4) step_kernel_tile(const StepArgs a) {
     using P = Pop<F16C>;
     using S = typename P::T;
     constexpr int Q = L::Q, D = L::D, K = D + 1;
