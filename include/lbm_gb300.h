@@ -217,6 +217,36 @@ lbm_status lbm_sum_link_force(lbm_handle* h, const float* link_force, int64_t n_
 lbm_status lbm_drag_force(lbm_handle* h, float* node_force, const void* f, const uint8_t* flags,
                           const int32_t* fluid_ids, int64_t n_nodes, void* stream);
 
+/* ---- batched persistent step ----
+ * No counterpart in the reference, whose grid sizes are compile-time parameters
+ * (src/lbm/grid.mojo:55-66), so one kernel launch steps one domain.  A batch steps many domains
+ * of different sizes (same lattice and config) in one persistent launch: every 256-cell tile of
+ * every domain is a work unit, and each domain is stepped exactly as lbm_*_step would step it
+ * (identical results).  Each grid needs a 256-cell tile with power-of-two sides and Q*N < 2^31. */
+typedef struct lbm_batch lbm_batch;
+
+lbm_status lbm_batch_create(const lbm_config_t* cfg, int32_t n_domains, const lbm_grid_t* grids,
+                            lbm_batch** out);
+lbm_status lbm_batch_destroy(lbm_batch* b);
+
+/* Buffers and tau of domain i (device pointers, the domain's own layout).  Double buffer: step k
+ * of lbm_batch_run reads f_a when (first_step + k) is even, else f_b.  Esoteric pull: f_b unused. */
+lbm_status lbm_batch_set_domain(lbm_batch* b, int32_t i, void* f_a, void* f_b, float* bc,
+                                const uint8_t* flags, float tau);
+
+/* Link-wise bounce-back after every batched step (interpolated_BB.mojo:46-141): device arrays of
+ * n_links entries, each link naming its domain; fluid_ids are flag-layout indices within that
+ * domain.  link_force (n_links*D floats, link fastest) may be NULL.  Double buffer only. */
+lbm_status lbm_batch_set_links(lbm_batch* b, const int32_t* domain, const int32_t* fluid_ids,
+                               const int32_t* dirs, const float* dists, int64_t n_links,
+                               int32_t method, float q_clamp, float* link_force);
+
+/* n_steps steps of every domain, replayed from a CUDA graph of 64 steps. */
+lbm_status lbm_batch_run(lbm_batch* b, int64_t n_steps, int64_t first_step, void* stream);
+
+/* Total cells of the batch (-1 for a null batch). */
+int64_t lbm_batch_cells(const lbm_batch* b);
+
 /* Float16C codec (src/utils/custom_fp.mojo:36-101) over device arrays. */
 lbm_status lbm_float16c_encode(const float* in, uint16_t* out, int64_t n, void* stream);
 lbm_status lbm_float16c_decode(const uint16_t* in, float* out, int64_t n, void* stream);

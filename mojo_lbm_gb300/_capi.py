@@ -68,6 +68,12 @@ SIGNATURES = {
     "lbm_linkwise_bounceback": (_i32, [_vp, _vp, _vp, _vp, _vp, _vp, _i64, _i32, _i32, _f32, _vp]),
     "lbm_sum_link_force": (_i32, [_vp, _vp, _i64, C.POINTER(C.c_double), _vp]),
     "lbm_drag_force": (_i32, [_vp, _vp, _vp, _vp, _vp, _i64, _vp]),
+    "lbm_batch_create": (_i32, [_CFG, _i32, _GRID, C.POINTER(_vp)]),
+    "lbm_batch_destroy": (_i32, [_vp]),
+    "lbm_batch_set_domain": (_i32, [_vp, _i32, _vp, _vp, _vp, _vp, _f32]),
+    "lbm_batch_set_links": (_i32, [_vp, _vp, _vp, _vp, _vp, _i64, _i32, _f32, _vp]),
+    "lbm_batch_run": (_i32, [_vp, _i64, _i64, _vp]),
+    "lbm_batch_cells": (_i64, [_vp]),
     "lbm_float16c_encode": (_i32, [_vp, _vp, _i64, _vp]),
     "lbm_float16c_decode": (_i32, [_vp, _vp, _i64, _vp]),
     "lbm_last_error": (C.c_char_p, []),

@@ -384,12 +384,10 @@ struct LinkArgs {
 // decoded as idx_to_ijk does (:24-43).  Float16C is decoded with use_float16c and the force adds
 // the weight under DDF shift (output/drag.mojo:88-93).
 template <class L, bool F16C>
-__global__ void link_kernel(const LinkArgs a) {
+__device__ __forceinline__ void link_one(const LinkArgs& a, const int64_t t) {
     using P = Pop<F16C>;
     using S = typename P::T;
     constexpr int Q = L::Q, D = L::D;
-    const int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-    if (t >= a.n) return;
     const uint32_t li = (uint32_t)a.ids[t];
     if (li >= a.lay.ncells) return;
     Nbr nb;
@@ -432,6 +430,13 @@ __global__ void link_kernel(const LinkArgs a) {
             a.force[t + a.n * dc.value] = (float)cd * (fa + fb);
         });
     }
+}
+
+template <class L, bool F16C>
+__global__ void link_kernel(const LinkArgs a) {
+    const int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= a.n) return;
+    link_one<L, F16C>(a, t);
 }
 
 struct DragArgs {

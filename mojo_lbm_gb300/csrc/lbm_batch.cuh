@@ -1,0 +1,126 @@
+// Batched persistent step: many domains of different size, one launch.
+//
+// Each domain is a complete single-domain problem (its own grid, tiled layout, f / bc / flags
+// buffers and tau), described by a StepArgs.  The work units are the 256-cell tiles of all
+// domains, numbered consecutively domain after domain.  A fixed grid of CTAs (SMs x resident
+// CTAs) takes equal contiguous ranges of units; a CTA keeps its current domain's StepArgs in
+// shared memory, reloads it when its range crosses into the next domain, and runs the same
+// block-per-tile body (tile_step) as the single-domain kernel, so a batched step equals the
+// single-domain steps bit for bit.  Two descriptor arrays hold the even and odd step of every
+// domain (buffers swapped, esoteric parity), so the kernel only picks one.
+#pragma once
+
+#include "lbm_aux.cuh"
+
+namespace lbm {
+
+struct BatchArgs {
+    const StepArgs* dom;          // ndom descriptors for this step's parity
+    const uint32_t* unit_begin;   // ndom + 1 offsets of the domains' first tile units
+    uint32_t ndom, total_units;
+};
+
+__device__ __forceinline__ uint32_t find_domain(const uint32_t* begin, uint32_t ndom, uint32_t u) {
+    uint32_t lo = 0, hi = ndom;  // begin[lo] <= u < begin[hi]
+    while (hi - lo > 1u) {
+        const uint32_t mid = (lo + hi) >> 1;
+        if (__ldg(begin + mid) <= u) lo = mid;
+        else hi = mid;
+    }
+    return lo;
+}
+
+template <class L, int METHOD, bool F16C, int COLL, bool LES>
+__global__ void __launch_bounds__(256, (L::Q == 9) ? 5 : ((COLL == LBM_KBC || L::Q == 27) ? 3 : 4)) step_kernel_batch(const BatchArgs b) {
+    __shared__ StepArgs sa;
+    // a contiguous, equal share of the units per CTA: the domain changes rarely along it, so the
+    // descriptor is reloaded only when it does
+    const uint32_t per = (b.total_units + gridDim.x - 1u) / gridDim.x;
+    const uint32_t u0 = blockIdx.x * per;
+    const uint32_t u1 = min(b.total_units, u0 + per);
+    if (u0 >= u1) return;
+    uint32_t d = find_domain(b.unit_begin, b.ndom, u0);
+    uint32_t loaded = 0xffffffffu;
+    uint32_t next_begin = __ldg(b.unit_begin + d + 1);
+    for (uint32_t u = u0; u < u1; ++u) {
+        while (u >= next_begin) {  // block-uniform
+            ++d;
+            next_begin = __ldg(b.unit_begin + d + 1);
+        }
+        if (d != loaded) {  // block-uniform
+            __syncthreads();  // every thread is done with the previous descriptor
+            const uint32_t* src = reinterpret_cast<const uint32_t*>(b.dom + d);
+            uint32_t* dst = reinterpret_cast<uint32_t*>(&sa);
+            for (uint32_t i = threadIdx.x; i < sizeof(StepArgs) / 4; i += blockDim.x) dst[i] = __ldg(src + i);
+            __syncthreads();
+            loaded = d;
+        }
+        tile_step<L, METHOD, F16C, COLL, LES>(sa, u - __ldg(b.unit_begin + d), threadIdx.x);
+    }
+}
+
+// tile_any of every unit of every domain; one warp per unit.
+__device__ __forceinline__ void batch_summary_unit(const BatchArgs& b, uint32_t u, uint32_t lane,
+                                                   uint8_t* tile_any) {
+    const uint32_t d = find_domain(b.unit_begin, b.ndom, u);
+    const StepArgs& a = b.dom[d];
+    const uint8_t* p = a.flags + (size_t)(u - b.unit_begin[d]) * a.lay.T;
+    uint32_t any = 0;
+    for (uint32_t i = lane; i < a.lay.T; i += 32) any |= __ldg(p + i);
+    any = __reduce_or_sync(0xffffffffu, any);
+    if (lane == 0) tile_any[u] = any != 0u;
+}
+
+struct BatchLinkArgs {
+    const StepArgs* dom;   // descriptors of the step that just ran: f_out is the lattice to fix
+    const int32_t* domain;
+    const int32_t* ids;
+    const int32_t* dirs;
+    const float* dists;
+    float* force;
+    int64_t n;
+    float q_clamp;
+    int32_t bouzidi, compute_force, ddf;
+};
+
+// linkwise_bounceback_kernel (src/lbm/geometry/interpolated_BB.mojo:46-141) over the links of all
+// domains: each link carries its domain, and works on that domain's freshly written lattice.
+template <class L, bool F16C>
+__global__ void link_kernel_batch(const BatchLinkArgs b) {
+    const int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= b.n) return;
+    const StepArgs& a = b.dom[b.domain[t]];
+    LinkArgs la;
+    la.lay = a.lay;
+    la.f = a.f_out;
+    la.force = b.force;
+    la.ids = b.ids;
+    la.dirs = b.dirs;
+    la.dists = b.dists;
+    la.n = b.n;
+    la.q_clamp = b.q_clamp;
+    la.bouzidi = b.bouzidi;
+    la.compute_force = b.compute_force;
+    la.ddf = b.ddf;
+    link_one<L, F16C>(la, t);
+}
+
+using BatchLaunch = cudaError_t (*)(const BatchArgs&, int sms, cudaStream_t);
+
+template <class L, int METHOD, bool F16C, int COLL, bool LES>
+cudaError_t launch_step_batch(const BatchArgs& b, int sms, cudaStream_t s) {
+    static int per_sm = 0;
+    if (per_sm == 0) {
+        const cudaError_t e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(
+            &per_sm, step_kernel_batch<L, METHOD, F16C, COLL, LES>, (int)kTileCells, 0);
+        if (e != cudaSuccess) return e;
+        if (per_sm < 1) per_sm = 1;
+    }
+    uint32_t grid = (uint32_t)(sms * per_sm);
+    if (grid > b.total_units) grid = b.total_units;
+    if (grid == 0) return cudaSuccess;
+    step_kernel_batch<L, METHOD, F16C, COLL, LES><<<grid, kTileCells, 0, s>>>(b);
+    return cudaGetLastError();
+}
+
+}  // namespace lbm

@@ -1,0 +1,319 @@
+// C ABI of the batched persistent step (lbm_batch_* in include/lbm_gb300.h).
+#include <cuda_runtime.h>
+
+#include <cstring>
+#include <map>
+#include <string>
+#include <vector>
+
+#include "lbm_batch.cuh"
+
+namespace lbm {
+void set_last_error(const char* msg);  // lbm_capi.cu
+BatchLaunch get_batch_step_d2q9(int, int, int, int);
+BatchLaunch get_batch_step_d3q19(int, int, int, int);
+BatchLaunch get_batch_step_d3q27(int, int, int, int);
+cudaError_t launch_link_batch_d2q9(const BatchLinkArgs&, bool, cudaStream_t);
+cudaError_t launch_link_batch_d3q19(const BatchLinkArgs&, bool, cudaStream_t);
+cudaError_t launch_link_batch_d3q27(const BatchLinkArgs&, bool, cudaStream_t);
+}  // namespace lbm
+
+using namespace lbm;
+
+extern "C" lbm_status lbm_validate(const lbm_config_t* cfg, const lbm_grid_t* grid);
+extern "C" const char* lbm_last_error(void);
+
+struct lbm_batch {
+    lbm_config_t cfg;
+    int32_t lattice;
+    int32_t ndom;
+    std::vector<lbm_grid_t> grids;
+    std::vector<StepArgs> even, odd;   // host descriptors per parity
+    std::vector<uint8_t> set;          // domain has buffers
+    std::vector<uint32_t> unit_begin;  // ndom + 1
+    StepArgs* d_even = nullptr;
+    StepArgs* d_odd = nullptr;
+    uint32_t* d_begin = nullptr;
+    uint8_t* d_tile_any = nullptr;
+    bool dirty = true;
+    BatchLaunch step = nullptr;
+    // links (caller-owned device arrays, concatenated over domains)
+    const int32_t *l_dom = nullptr, *l_ids = nullptr, *l_dirs = nullptr;
+    const float* l_dists = nullptr;
+    float* l_force = nullptr;
+    int64_t n_links = 0;
+    int32_t l_method = LBM_BB_BOUZIDI;
+    float l_qclamp = 0.f;
+    int sms = 1;
+    cudaStream_t capture_stream = nullptr;
+    std::map<int, cudaGraphExec_t> graphs;  // keyed by the parity of the first step
+};
+
+namespace {
+
+lbm_status bfail(lbm_status s, const std::string& m) {
+    set_last_error(m.c_str());
+    return s;
+}
+
+#define LBM_BCK(call)                                                                          \
+    do {                                                                                       \
+        cudaError_t e_ = (call);                                                               \
+        if (e_ != cudaSuccess) return bfail(LBM_ECUDA, std::string(#call) + ": " + cudaGetErrorString(e_)); \
+    } while (0)
+
+bool pow2(int v) { return v > 0 && (v & (v - 1)) == 0; }
+int ilog2(int v) { int r = 0; while ((1 << r) < v) ++r; return r; }
+
+void drop_graphs(lbm_batch* b) {
+    for (auto& kv : b->graphs) cudaGraphExecDestroy(kv.second);
+    b->graphs.clear();
+}
+
+__global__ void batch_summary_kernel(const BatchArgs b, uint8_t* tile_any) {
+    const uint32_t warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, lane = threadIdx.x & 31;
+    if (warp >= b.total_units) return;
+    batch_summary_unit(b, warp, lane, tile_any);
+}
+
+lbm_status launch_links(lbm_batch* b, const StepArgs* dom, cudaStream_t s) {
+    if (b->n_links == 0) return LBM_OK;
+    BatchLinkArgs la;
+    la.dom = dom;
+    la.domain = b->l_dom;
+    la.ids = b->l_ids;
+    la.dirs = b->l_dirs;
+    la.dists = b->l_dists;
+    la.force = b->l_force;
+    la.n = b->n_links;
+    la.q_clamp = b->l_qclamp;
+    la.bouzidi = b->l_method == LBM_BB_BOUZIDI;
+    la.compute_force = b->l_force != nullptr;
+    la.ddf = b->cfg.DDF_shift;
+    const bool f16 = b->cfg.use_float16c != 0;
+    cudaError_t e = b->lattice == LBM_D2Q9 ? launch_link_batch_d2q9(la, f16, s)
+                  : b->lattice == LBM_D3Q19 ? launch_link_batch_d3q19(la, f16, s)
+                                            : launch_link_batch_d3q27(la, f16, s);
+    LBM_BCK(e);
+    return LBM_OK;
+}
+
+// One step of every domain: the persistent step kernel, then the link-wise bounce-back.
+lbm_status batch_step(lbm_batch* b, bool parity_odd, cudaStream_t s) {
+    BatchArgs a;
+    a.dom = parity_odd ? b->d_odd : b->d_even;
+    a.unit_begin = b->d_begin;
+    a.ndom = (uint32_t)b->ndom;
+    a.total_units = b->unit_begin.back();
+    LBM_BCK(b->step(a, b->sms, s));
+    return launch_links(b, a.dom, s);
+}
+
+}  // namespace
+
+extern "C" {
+
+lbm_status lbm_batch_create(const lbm_config_t* cfg, int32_t n_domains, const lbm_grid_t* grids, lbm_batch** out) {
+    if (!out) return bfail(LBM_EINVAL, "null output pointer");
+    *out = nullptr;
+    if (!cfg || !grids || n_domains <= 0) return bfail(LBM_EINVAL, "need a config and at least one grid");
+    const int32_t lat = grids[0].lattice;
+    uint64_t units = 0;
+    std::vector<uint32_t> begin(n_domains + 1, 0);
+    for (int32_t i = 0; i < n_domains; ++i) {
+        const lbm_grid_t& g = grids[i];
+        const lbm_status v = lbm_validate(cfg, &g);
+        if (v != LBM_OK) return bfail(v, "domain " + std::to_string(i) + ": " + lbm_last_error());
+        if (g.lattice != lat) return bfail(LBM_EINVAL, "all domains of a batch must use the same lattice");
+        const int64_t Q = lat == LBM_D2Q9 ? 9 : lat == LBM_D3Q19 ? 19 : 27;
+        const int64_t N = (int64_t)g.nx * g.ny * g.nz;
+        if ((int64_t)g.tx * g.ty * g.tz != (int64_t)kTileCells || !pow2(g.tx) || !pow2(g.ty) || !pow2(g.tz) ||
+            Q * N >= ((int64_t)1 << 31))
+            return bfail(LBM_EUNSUPPORTED, "domain " + std::to_string(i) +
+                                               ": batched domains need 256-cell tiles with power-of-two sides "
+                                               "and Q*N < 2^31");
+        begin[i] = (uint32_t)units;
+        units += (uint64_t)(N / kTileCells);
+    }
+    if (units >= ((uint64_t)1 << 32)) return bfail(LBM_EINVAL, "too many tiles in the batch");
+    begin[n_domains] = (uint32_t)units;
+
+    lbm_batch* b = new lbm_batch();
+    b->cfg = *cfg;
+    b->lattice = lat;
+    b->ndom = n_domains;
+    b->grids.assign(grids, grids + n_domains);
+    b->unit_begin = begin;
+    b->even.resize(n_domains);
+    b->odd.resize(n_domains);
+    b->set.assign(n_domains, 0);
+    const int m = cfg->lbm_method, f16 = cfg->use_float16c ? 1 : 0, co = cfg->collision_op, les = cfg->LES ? 1 : 0;
+    b->step = lat == LBM_D2Q9 ? get_batch_step_d2q9(m, f16, co, les)
+            : lat == LBM_D3Q19 ? get_batch_step_d3q19(m, f16, co, les)
+                               : get_batch_step_d3q27(m, f16, co, les);
+    int dev = 0;
+    cudaError_t e = cudaGetDevice(&dev);
+    if (e == cudaSuccess) e = cudaDeviceGetAttribute(&b->sms, cudaDevAttrMultiProcessorCount, dev);
+    if (e == cudaSuccess) e = cudaMalloc(&b->d_even, sizeof(StepArgs) * n_domains);
+    if (e == cudaSuccess) e = cudaMalloc(&b->d_odd, sizeof(StepArgs) * n_domains);
+    if (e == cudaSuccess) e = cudaMalloc(&b->d_begin, sizeof(uint32_t) * (n_domains + 1));
+    if (e == cudaSuccess) e = cudaMalloc(&b->d_tile_any, units > 0 ? units : 1);
+    if (e == cudaSuccess)
+        e = cudaMemcpy(b->d_begin, begin.data(), sizeof(uint32_t) * (n_domains + 1), cudaMemcpyHostToDevice);
+    if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&b->capture_stream, cudaStreamNonBlocking);
+    if (e != cudaSuccess) {
+        lbm_batch_destroy(b);
+        return bfail(LBM_ECUDA, std::string("lbm_batch_create: ") + cudaGetErrorString(e));
+    }
+    *out = b;
+    return LBM_OK;
+}
+
+lbm_status lbm_batch_destroy(lbm_batch* b) {
+    if (!b) return LBM_OK;
+    drop_graphs(b);
+    cudaFree(b->d_even);
+    cudaFree(b->d_odd);
+    cudaFree(b->d_begin);
+    cudaFree(b->d_tile_any);
+    if (b->capture_stream) cudaStreamDestroy(b->capture_stream);
+    delete b;
+    return LBM_OK;
+}
+
+lbm_status lbm_batch_set_domain(lbm_batch* b, int32_t i, void* f_a, void* f_b, float* bc, const uint8_t* flags,
+                                float tau) {
+    if (!b) return bfail(LBM_EINVAL, "null batch");
+    if (i < 0 || i >= b->ndom) return bfail(LBM_EINVAL, "domain index out of range");
+    const bool eso = b->cfg.lbm_method == LBM_ESOTERIC_PULL;
+    if (!f_a || !flags || (!eso && (!f_b || f_a == f_b))) return bfail(LBM_EINVAL, "bad buffers for the domain");
+    if (!bc && (b->cfg.include_moving_boundary || b->cfg.include_equilibrium_bc || b->cfg.capture_density ||
+                b->cfg.capture_velocity))
+        return bfail(LBM_EINVAL, "bc is required by this configuration");
+    const lbm_grid_t& g = b->grids[i];
+    StepArgs a;
+    std::memset(&a, 0, sizeof(a));
+    a.lay.nx = g.nx; a.lay.ny = g.ny; a.lay.nz = g.nz;
+    a.lay.tx = g.tx; a.lay.ty = g.ty; a.lay.tz = g.tz;
+    a.lay.ntx = g.nx / g.tx; a.lay.nty = g.ny / g.ty; a.lay.ntz = g.nz / g.tz;
+    a.lay.T = kTileCells;
+    a.lay.ncells = (uint32_t)((int64_t)g.nx * g.ny * g.nz);
+    a.lay.d_tx = FastDiv((uint32_t)g.tx);
+    a.lay.d_ty = FastDiv((uint32_t)g.ty);
+    a.lay.d_T = FastDiv(kTileCells);
+    a.lay.d_ntx = FastDiv((uint32_t)a.lay.ntx);
+    a.lay.d_nty = FastDiv((uint32_t)a.lay.nty);
+    a.bc = bc;
+    a.flags = flags;
+    a.tau = tau;
+    a.Cs = b->cfg.Cs;
+    a.trt_lambda = b->cfg.trt_lambda;
+    a.ddf = b->cfg.DDF_shift;
+    a.moving = b->cfg.include_moving_boundary;
+    a.eqbc = b->cfg.include_equilibrium_bc;
+    a.cap_rho = b->cfg.capture_density;
+    a.cap_u = b->cfg.capture_velocity;
+    a.tile_any = b->d_tile_any + b->unit_begin[i];
+    a.mx = (uint32_t)g.tx - 1u;
+    a.my = (uint32_t)g.ty - 1u;
+    a.shx = (uint32_t)ilog2(g.tx);
+    a.shxy = (uint32_t)(ilog2(g.tx) + ilog2(g.ty));
+    StepArgs ev = a, od = a;
+    if (eso) {
+        ev.f_in = ev.f_out = f_a;
+        od.f_in = od.f_out = f_a;
+        ev.even = 1;
+        od.even = 0;
+    } else {
+        ev.f_in = f_a; ev.f_out = f_b;
+        od.f_in = f_b; od.f_out = f_a;
+    }
+    b->even[i] = ev;
+    b->odd[i] = od;
+    b->set[i] = 1;
+    b->dirty = true;
+    return LBM_OK;
+}
+
+lbm_status lbm_batch_set_links(lbm_batch* b, const int32_t* domain, const int32_t* fluid_ids, const int32_t* dirs,
+                               const float* dists, int64_t n_links, int32_t method, float q_clamp, float* link_force) {
+    if (!b) return bfail(LBM_EINVAL, "null batch");
+    if (n_links < 0) return bfail(LBM_EINVAL, "n_links must be non-negative");
+    if (n_links > 0 && b->cfg.lbm_method != LBM_DOUBLE_BUFFER)
+        return bfail(LBM_EUNSUPPORTED, "linkwise bounce-back needs the double-buffer method");
+    if (n_links > 0 && (!domain || !fluid_ids || !dirs || !dists)) return bfail(LBM_EINVAL, "null link array");
+    if (method != LBM_BB_MID_GRID && method != LBM_BB_BOUZIDI) return bfail(LBM_EINVAL, "unknown bounce-back method");
+    b->l_dom = domain;
+    b->l_ids = fluid_ids;
+    b->l_dirs = dirs;
+    b->l_dists = dists;
+    b->l_force = link_force;
+    b->n_links = n_links;
+    b->l_method = method;
+    b->l_qclamp = q_clamp;
+    drop_graphs(b);
+    return LBM_OK;
+}
+
+lbm_status lbm_batch_run(lbm_batch* b, int64_t n_steps, int64_t first_step, void* stream) {
+    if (!b) return bfail(LBM_EINVAL, "null batch");
+    if (n_steps < 0 || first_step < 0) return bfail(LBM_EINVAL, "n_steps and first_step must be non-negative");
+    for (int32_t i = 0; i < b->ndom; ++i)
+        if (!b->set[i]) return bfail(LBM_EINVAL, "domain " + std::to_string(i) + " has no buffers");
+    cudaStream_t s = (cudaStream_t)stream;
+    if (n_steps == 0) return LBM_OK;
+    if (b->dirty) {
+        LBM_BCK(cudaMemcpyAsync(b->d_even, b->even.data(), sizeof(StepArgs) * b->ndom, cudaMemcpyHostToDevice, s));
+        LBM_BCK(cudaMemcpyAsync(b->d_odd, b->odd.data(), sizeof(StepArgs) * b->ndom, cudaMemcpyHostToDevice, s));
+        LBM_BCK(cudaStreamSynchronize(s));  // the host descriptors may change after return
+        b->dirty = false;
+    }
+    {
+        BatchArgs a;
+        a.dom = b->d_even;
+        a.unit_begin = b->d_begin;
+        a.ndom = (uint32_t)b->ndom;
+        a.total_units = b->unit_begin.back();
+        const uint32_t blocks = (uint32_t)(((uint64_t)a.total_units * 32 + 255) / 256);
+        if (blocks) batch_summary_kernel<<<blocks, 256, 0, s>>>(a, b->d_tile_any);
+        LBM_BCK(cudaGetLastError());
+    }
+    const int64_t chunk = 64;
+    int64_t done = 0;
+    if (n_steps >= chunk) {
+        const int key = (int)(first_step % 2);
+        auto it = b->graphs.find(key);
+        if (it == b->graphs.end()) {
+            cudaGraph_t g = nullptr;
+            LBM_BCK(cudaStreamBeginCapture(b->capture_stream, cudaStreamCaptureModeThreadLocal));
+            lbm_status st = LBM_OK;
+            for (int64_t k = 0; k < chunk && st == LBM_OK; ++k)
+                st = batch_step(b, ((first_step + k) % 2) != 0, b->capture_stream);
+            cudaError_t e = cudaStreamEndCapture(b->capture_stream, &g);
+            if (st != LBM_OK || e != cudaSuccess) {
+                if (g) cudaGraphDestroy(g);
+                return st != LBM_OK ? st : bfail(LBM_ECUDA, "lbm_batch_run: graph capture failed");
+            }
+            cudaGraphExec_t ge = nullptr;
+            e = cudaGraphInstantiate(&ge, g, 0);
+            cudaGraphDestroy(g);
+            if (e != cudaSuccess) return bfail(LBM_ECUDA, std::string("lbm_batch_run: ") + cudaGetErrorString(e));
+            it = b->graphs.emplace(key, ge).first;
+        }
+        for (; done + chunk <= n_steps; done += chunk) LBM_BCK(cudaGraphLaunch(it->second, s));
+    }
+    for (; done < n_steps; ++done) {
+        const lbm_status st = batch_step(b, ((first_step + done) % 2) != 0, s);
+        if (st != LBM_OK) return st;
+    }
+    return LBM_OK;
+}
+
+int64_t lbm_batch_cells(const lbm_batch* b) {
+    if (!b) return -1;
+    int64_t n = 0;
+    for (const auto& g : b->grids) n += (int64_t)g.nx * g.ny * g.nz;
+    return n;
+}
+
+}  // extern "C"

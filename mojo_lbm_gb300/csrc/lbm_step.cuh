@@ -470,15 +470,16 @@ __global__ void __launch_bounds__(256) step_kernel(const StepArgs a) {
 // ---------------------------------------------------------------------------------------------
 constexpr uint32_t kTileCells = 256;
 
+// The per-thread body of the block-per-tile step: thread `tid` of the CTA that owns tile `tile`.
+// Every lane of a warp must call it (it starts with a warp ballot).
 template <class L, int METHOD, bool F16C, int COLL, bool LES>
-__global__ void __launch_bounds__(256, (COLL == LBM_KBC || L::Q == 27) ? 3 : 4) step_kernel_tile(const StepArgs a) {
+__device__ __forceinline__ void tile_step(const StepArgs& a, const uint32_t tile, const uint32_t tid) {
     using P = Pop<F16C>;
     using S = typename P::T;
     constexpr int Q = L::Q, D = L::D, K = D + 1;
     constexpr uint32_t T = kTileCells;
     constexpr bool ESO = METHOD == LBM_ESOTERIC_PULL;
 
-    const uint32_t tile = blockIdx.x, tid = threadIdx.x;
     const uint32_t n = tid + T * tile;  // cell index = flag offset
     const uint32_t byz = a.lay.d_ntx.div(tile);
     const uint32_t bx = tile - byz * (uint32_t)a.lay.ntx;
@@ -616,6 +617,11 @@ __global__ void __launch_bounds__(256, (COLL == LBM_KBC || L::Q == 27) ? 3 : 4) 
             P::st(foA + own + (int32_t)(T * pos), f[neg]);
         });
     }
+}
+
+template <class L, int METHOD, bool F16C, int COLL, bool LES>
+__global__ void __launch_bounds__(256, (L::Q == 9) ? 5 : ((COLL == LBM_KBC || L::Q == 27) ? 3 : 4)) step_kernel_tile(const StepArgs a) {
+    tile_step<L, METHOD, F16C, COLL, LES>(a, blockIdx.x, threadIdx.x);
 }
 
 // Launcher type used by the dispatch tables.

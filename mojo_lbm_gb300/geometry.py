@@ -86,21 +86,16 @@ def get_rigid_sphere(grid, flags_host: np.ndarray, center, radius: float, device
     flags_host[lay.flag_offset(X[inside], Y[inside], Z[inside])] = Flags.SOLID
     fx, fy, fz = X[~inside], Y[~inside], Z[~inside]
     xf = P[~inside]
-    ids, dirs, dists, uniq = [], [], [], []
-    dirs_c = grid.lattice.directions
-    for k in range(len(fx)):
-        fid = int(lay.flag_offset(fx[k], fy[k], fz[k]))
-        first = True
-        for q in range(Q):
-            t = [fx[k], fy[k], fz[k]]
-            for i in range(D):
-                t[i] += int(dirs_c[q][i])
-            xs = np.asarray(grid.get_grid_coordinates(*t), dtype=np.float64)
-            if ((xs - c) ** 2).sum() <= radius ** 2:
-                if first:
-                    uniq.append(fid)
-                    first = False
-                ids.append(fid)
-                dirs.append(q)
-                dists.append(float(get_q_for_sphere(xf[k], xs, c, radius)))
+    # every (fluid candidate, direction) pair whose neighbour lies inside the sphere is a link
+    cdirs = grid.lattice.directions.astype(np.int64)                      # [Q, D]
+    nb = np.stack([fx, fy, fz], -1)[:, None, :].repeat(Q, 1).astype(np.int64)
+    nb[..., :D] += cdirs[None, :, :]
+    xs = np.stack(grid.get_grid_coordinates(nb[..., 0], nb[..., 1], nb[..., 2]), -1)   # [n, Q, 3]
+    hit = ((xs - c) ** 2).sum(-1) <= radius ** 2                          # [n, Q]
+    k_idx, q_idx = np.nonzero(hit)                                        # ordered by node, then q
+    fid = lay.flag_offset(fx, fy, fz).astype(np.int64)
+    ids = fid[k_idx]
+    dirs = q_idx
+    dists = get_q_for_sphere(xf[k_idx], xs[k_idx, q_idx], c, radius) if len(k_idx) else np.zeros(0)
+    uniq = fid[np.unique(k_idx)]
     return RigidStationaryObject(grid, uniq, ids, dirs, dists, device)
