@@ -247,6 +247,51 @@ lbm_status lbm_batch_run(lbm_batch* b, int64_t n_steps, int64_t first_step, void
 /* Total cells of the batch (-1 for a null batch). */
 int64_t lbm_batch_cells(const lbm_batch* b);
 
+/* ---- learned subgrid closure ----
+ * No counterpart in the reference, whose LES is Smagorinsky with Cs = 0.1
+ * (ops/turbulence.mojo:12-38).  A per-cell MLP 8 -> 32 -> 32 -> 1 (ReLU hidden layers, softplus
+ * output) maps invariants of the non-equilibrium strain, rho and |u| to an eddy viscosity
+ * nu_t = softplus(y) * nu_scale; tau_eddy = 3 nu_t replaces Smagorinsky's.  Cells whose
+ * normalised features leave [feat_lo, feat_hi] (the training range) keep Smagorinsky.  Inference
+ * runs inside the collision of LES configurations on the tensor cores (BF16 weights and
+ * activations, FP32 accumulation).  Features, with S the strain rate from the non-equilibrium
+ * stress (moment.mojo:154-176), s2 its squared norm (off-diagonals twice), |S| = sqrt(2 s2):
+ *   x0 log(|S| + 1e-12)          x1 tr(S) / (|S| + 1e-12)
+ *   x2 det(S_dev) / (|S|^3 + 1e-30)   x3 rho - 1
+ *   x4 |u|                       x5 2 (Sxy^2 + Sxz^2 + Syz^2) / (s2 + 1e-30)
+ *   x6 log(tau - 0.5)            x7 |u|^2 / (|S| + 1e-12)
+ * normalised as (x - feat_mean) * feat_scale.  Weights are stored input-major:
+ * w1[k*32 + j] links input k to hidden unit j, w2[k*32 + j] likewise, w3[k] hidden k to y. */
+typedef struct lbm_closure_t {
+    float w1[8 * 32];
+    float b1[32];
+    float w2[32 * 32];
+    float b2[32];
+    float w3[32];
+    float b3;
+    float nu_scale;
+    float feat_mean[8];
+    float feat_scale[8];
+    float feat_lo[8];
+    float feat_hi[8];
+} lbm_closure_t;
+
+/* Use the learned closure in an LES handle (copied; NULL returns to Smagorinsky).  Waits for the
+ * device to be idle first: call it between steps. */
+lbm_status lbm_set_closure(lbm_handle* h, const lbm_closure_t* closure);
+
+/* Training kernels of the closure (float32).  theta: the 1377 parameters packed as
+ * w1, b1, w2, b2, w3, b3.  x: n rows of 8 normalised features; nu: n outputs
+ * softplus(y) * nu_scale.  lbm_mlp_backward writes d(sum_i g_i nu_i)/d theta into grad_theta
+ * (summed in a fixed order: repeatable).  lbm_mlp_adam applies one Adam step to n_params
+ * parameters with moments m, v (t = step count from 1). */
+lbm_status lbm_mlp_forward(const float* theta, const float* x, int64_t n, float nu_scale, float* nu,
+                           void* stream);
+lbm_status lbm_mlp_backward(const float* theta, const float* x, const float* g, int64_t n,
+                            float nu_scale, float* grad_theta, void* stream);
+lbm_status lbm_mlp_adam(float* theta, const float* grad, float* m, float* v, int32_t n_params,
+                        float lr, float beta1, float beta2, float eps, int32_t t, void* stream);
+
 /* Float16C codec (src/utils/custom_fp.mojo:36-101) over device arrays. */
 lbm_status lbm_float16c_encode(const float* in, uint16_t* out, int64_t n, void* stream);
 lbm_status lbm_float16c_decode(const uint16_t* in, float* out, int64_t n, void* stream);

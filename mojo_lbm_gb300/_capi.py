@@ -37,6 +37,13 @@ class lbm_grid_t(C.Structure):
                 ("tx", C.c_int32), ("ty", C.c_int32), ("tz", C.c_int32)]
 
 
+class lbm_closure_t(C.Structure):
+    _fields_ = [("w1", C.c_float * 256), ("b1", C.c_float * 32), ("w2", C.c_float * 1024), ("b2", C.c_float * 32),
+                ("w3", C.c_float * 32), ("b3", C.c_float), ("nu_scale", C.c_float),
+                ("feat_mean", C.c_float * 8), ("feat_scale", C.c_float * 8), ("feat_lo", C.c_float * 8),
+                ("feat_hi", C.c_float * 8)]
+
+
 _vp = C.c_void_p
 _i32 = C.c_int32
 _i64 = C.c_int64
@@ -74,6 +81,10 @@ SIGNATURES = {
     "lbm_batch_set_links": (_i32, [_vp, _vp, _vp, _vp, _vp, _i64, _i32, _f32, _vp]),
     "lbm_batch_run": (_i32, [_vp, _i64, _i64, _vp]),
     "lbm_batch_cells": (_i64, [_vp]),
+    "lbm_set_closure": (_i32, [_vp, C.POINTER(lbm_closure_t)]),
+    "lbm_mlp_forward": (_i32, [_vp, _vp, _i64, _f32, _vp, _vp]),
+    "lbm_mlp_backward": (_i32, [_vp, _vp, _vp, _i64, _f32, _vp, _vp]),
+    "lbm_mlp_adam": (_i32, [_vp, _vp, _vp, _vp, _i32, _f32, _f32, _f32, _f32, _i32, _vp]),
     "lbm_float16c_encode": (_i32, [_vp, _vp, _i64, _vp]),
     "lbm_float16c_decode": (_i32, [_vp, _vp, _i64, _vp]),
     "lbm_last_error": (C.c_char_p, []),

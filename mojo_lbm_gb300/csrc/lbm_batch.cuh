@@ -30,7 +30,7 @@ __device__ __forceinline__ uint32_t find_domain(const uint32_t* begin, uint32_t 
     return lo;
 }
 
-template <class L, int METHOD, bool F16C, int COLL, bool LES>
+template <class L, int METHOD, bool F16C, int COLL, int LES>
 __global__ void __launch_bounds__(256, (L::Q == 9) ? 5 : ((COLL == LBM_KBC || L::Q == 27) ? 3 : 4)) step_kernel_batch(const BatchArgs b) {
     __shared__ StepArgs sa;
     // a contiguous, equal share of the units per CTA: the domain changes rarely along it, so the
@@ -107,7 +107,7 @@ __global__ void link_kernel_batch(const BatchLinkArgs b) {
 
 using BatchLaunch = cudaError_t (*)(const BatchArgs&, int sms, cudaStream_t);
 
-template <class L, int METHOD, bool F16C, int COLL, bool LES>
+template <class L, int METHOD, bool F16C, int COLL, int LES>
 cudaError_t launch_step_batch(const BatchArgs& b, int sms, cudaStream_t s) {
     static int per_sm = 0;
     if (per_sm == 0) {

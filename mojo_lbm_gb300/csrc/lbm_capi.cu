@@ -19,6 +19,10 @@ StepLaunch get_step_d3q27(int, int, int, int);
 StepLaunch get_tile_step_d2q9(int, int, int, int);
 StepLaunch get_tile_step_d3q19(int, int, int, int);
 StepLaunch get_tile_step_d3q27(int, int, int, int);
+StepLaunch get_learned_step_d2q9(int, int, int);
+StepLaunch get_learned_step_d3q19(int, int, int);
+StepLaunch get_learned_step_d3q27(int, int, int);
+void pack_closure(const lbm_closure_t& c, ClosureDev& d);
 }  // namespace lbm
 
 using namespace lbm;
@@ -71,6 +75,7 @@ struct lbm_handle {
     LayoutDesc lay;
     StepLaunch step;       // generic kernel (any tile)
     StepLaunch step_tile;  // block-per-tile kernel, or null when the grid does not qualify
+    StepLaunch step_learned;  // block-per-tile kernel with the learned closure (LES handles), or null
     int path;              // 0 auto, 1 generic only, 2 block-per-tile only
     uint8_t* tile_any;     // per-tile "has a non-FLUID flag" bytes for the block-per-tile kernel
     uint32_t ntiles;
@@ -79,6 +84,8 @@ struct lbm_handle {
     int device;
     int sm_count;
     double* scratch;  // kReduceBlocks*4 partials + 4 results
+    ClosureDev* closure;  // device copy of the learned closure's fragments, or null
+    int closure_on;
     cudaStream_t capture_stream;
     std::map<GraphKey, cudaGraphExec_t> graphs;
 };
@@ -117,6 +124,7 @@ StepArgs step_args(const lbm_handle* h, const void* f_in, void* f_out, float* bc
     a.cap_rho = h->cfg.capture_density;
     a.cap_u = h->cfg.capture_velocity;
     a.even = even;
+    a.closure = h->closure_on ? h->closure : nullptr;
     a.tile_any = h->tile_any;
     a.mx = h->mx;
     a.my = h->my;
@@ -126,6 +134,12 @@ StepArgs step_args(const lbm_handle* h, const void* f_in, void* f_out, float* bc
 }
 
 bool use_tile(const lbm_handle* h) { return h->step_tile != nullptr && h->path != 1; }
+
+// The kernel the next step runs.
+StepLaunch step_fn(const lbm_handle* h) {
+    if (!use_tile(h)) return h->step;
+    return h->closure_on ? h->step_learned : h->step_tile;
+}
 
 // Rebuilds the per-tile summary of `flags` for the block-per-tile kernel.
 lbm_status tile_summary(lbm_handle* h, const uint8_t* flags, cudaStream_t s) {
@@ -152,10 +166,8 @@ lbm_status step_once(lbm_handle* h, const void* f_in, void* f_out, float* bc, co
             const lbm_status st = tile_summary(h, flags, s);
             if (st != LBM_OK) return st;
         }
-        LBM_CK(h->step_tile(a, h->threads, s));
-    } else {
-        LBM_CK(h->step(a, h->threads, s));
     }
+    LBM_CK(step_fn(h)(a, h->threads, s));
     return LBM_OK;
 }
 
@@ -251,6 +263,10 @@ lbm_status lbm_create(const lbm_config_t* cfg, const lbm_grid_t* grid, lbm_handl
                  : grid->lattice == LBM_D2Q9 ? get_tile_step_d2q9(m, f16, co, les)
                  : grid->lattice == LBM_D3Q19 ? get_tile_step_d3q19(m, f16, co, les)
                                               : get_tile_step_d3q27(m, f16, co, les);
+    h->step_learned = !(tile_ok && les) ? nullptr
+                    : grid->lattice == LBM_D2Q9 ? get_learned_step_d2q9(m, f16, co)
+                    : grid->lattice == LBM_D3Q19 ? get_learned_step_d3q19(m, f16, co)
+                                                 : get_learned_step_d3q27(m, f16, co);
     h->path = 0;
     h->ntiles = h->lay.ncells / h->lay.T;
     h->mx = (uint32_t)grid->tx - 1u;
@@ -260,6 +276,8 @@ lbm_status lbm_create(const lbm_config_t* cfg, const lbm_grid_t* grid, lbm_handl
     h->tile_any = nullptr;
     h->threads = 256;
     h->scratch = nullptr;
+    h->closure = nullptr;
+    h->closure_on = 0;
     h->capture_stream = nullptr;
     cudaError_t e = cudaGetDevice(&h->device);
     if (e == cudaSuccess) e = cudaDeviceGetAttribute(&h->sm_count, cudaDevAttrMultiProcessorCount, h->device);
@@ -279,8 +297,38 @@ lbm_status lbm_destroy(lbm_handle* h) {
     for (auto& kv : h->graphs) cudaGraphExecDestroy(kv.second);
     if (h->scratch) cudaFree(h->scratch);
     if (h->tile_any) cudaFree(h->tile_any);
+    if (h->closure) cudaFree(h->closure);
     if (h->capture_stream) cudaStreamDestroy(h->capture_stream);
     delete h;
+    return LBM_OK;
+}
+
+lbm_status lbm_set_closure(lbm_handle* h, const lbm_closure_t* closure) {
+    if (check_handle(h)) return LBM_EINVAL;
+    if (closure && !h->cfg.LES)
+        return fail(LBM_EUNSUPPORTED, "the learned closure replaces Smagorinsky: the configuration needs LES");
+    if (closure && (!h->step_learned || h->path == 1))
+        return fail(LBM_EUNSUPPORTED, "the learned closure runs in the block-per-tile kernel: 256-cell "
+                                      "power-of-two tiles, Q*N < 2^31, kernel path not forced to generic");
+    if (closure) {
+        const float* p = reinterpret_cast<const float*>(closure);
+        for (size_t i = 0; i < sizeof(lbm_closure_t) / sizeof(float); ++i)
+            if (!std::isfinite(p[i])) return fail(LBM_EINVAL, "closure parameters must be finite");
+        if (!(closure->nu_scale >= 0.f)) return fail(LBM_EINVAL, "nu_scale must be non-negative");
+    }
+    // steps in flight may read the current fragments; graphs hold the old descriptor
+    LBM_CK(cudaDeviceSynchronize());
+    for (auto& kv : h->graphs) cudaGraphExecDestroy(kv.second);
+    h->graphs.clear();
+    if (!closure) {
+        h->closure_on = 0;
+        return LBM_OK;
+    }
+    ClosureDev d;
+    pack_closure(*closure, d);
+    if (!h->closure) LBM_CK(cudaMalloc(&h->closure, sizeof(ClosureDev)));
+    LBM_CK(cudaMemcpy(h->closure, &d, sizeof(ClosureDev), cudaMemcpyHostToDevice));
+    h->closure_on = 1;
     return LBM_OK;
 }
 
@@ -298,6 +346,8 @@ lbm_status lbm_set_kernel_path(lbm_handle* h, int32_t path) {
     if (path < 0 || path > 2) return fail(LBM_EINVAL, "path must be 0 (auto), 1 (generic) or 2 (block-per-tile)");
     if (path == 2 && !h->step_tile)
         return fail(LBM_EUNSUPPORTED, "the block-per-tile kernel needs 256-cell power-of-two tiles and Q*N < 2^31");
+    if (path == 1 && h->closure_on)
+        return fail(LBM_EUNSUPPORTED, "the learned closure runs in the block-per-tile kernel only");
     h->path = path;
     return LBM_OK;
 }
@@ -367,7 +417,7 @@ lbm_status lbm_run(lbm_handle* h, void* f_a, void* f_b, float* bc, const uint8_t
                 const StepArgs a = eso ? step_args(h, f_a, f_a, bc, flags, tau, a_is_src ? 1 : 0)
                                        : (a_is_src ? step_args(h, f_a, f_b, bc, flags, tau, 0)
                                                    : step_args(h, f_b, f_a, bc, flags, tau, 0));
-                const StepLaunch fn = use_tile(h) ? h->step_tile : h->step;
+                const StepLaunch fn = step_fn(h);
                 if (fn(a, h->threads, h->capture_stream) != cudaSuccess) st = LBM_ECUDA;
             }
             cudaError_t e = cudaStreamEndCapture(h->capture_stream, &g);

@@ -13,9 +13,13 @@
 // registers, unrolled at compile time over q as the reference does with `comptime for`.
 #pragma once
 
+#include "lbm_closure.cuh"
 #include "lbm_device.cuh"
 
 namespace lbm {
+
+// LES template argument of the step kernels.
+constexpr int kLesOff = 0, kLesSmagorinsky = 1, kLesLearned = 2;
 
 struct StepArgs {
     LayoutDesc lay;
@@ -26,6 +30,7 @@ struct StepArgs {
     float tau, Cs, trt_lambda;
     int32_t ddf, moving, eqbc, cap_rho, cap_u, even;
     // block-per-tile path (256-cell tiles with power-of-two sides)
+    const ClosureDev* closure; // learned LES closure, or null for Smagorinsky
     const uint8_t* tile_any;   // per tile: 1 if any flag of the tile is not FLUID (0)
     uint32_t mx, my, shx, shxy; // lx = t & mx, ly = (t >> shx) & my, lz = t >> shxy
 };
@@ -160,10 +165,13 @@ __device__ __forceinline__ float kbc_shear(const float* P) {
     }
 }
 
-// collide (src/lbm/kernels/steps/collide.mojo:23-90)
-template <class L, int COLL, bool LES>
+// collide (src/lbm/kernels/steps/collide.mojo:23-90).  LES: 0 off, kLesSmagorinsky, or
+// kLesLearned (the closure `cl` in shared memory, evaluated by every thread of the block; `active`
+// is false for the lanes kept alive only for it, which write nothing).
+template <class L, int COLL, int LES>
 __device__ __forceinline__ void collide(float (&f)[L::Q], float tau, const StepArgs& a, float* bc_own_base,
-                                        uint32_t T, uint8_t own_flag) {
+                                        uint32_t T, uint8_t own_flag, bool active = true,
+                                        const ClosureDev* cl = nullptr) {
     constexpr int Q = L::Q, D = L::D;
     const bool ddf = a.ddf != 0;
     float rho = 0.f;
@@ -183,8 +191,8 @@ __device__ __forceinline__ void collide(float (&f)[L::Q], float tau, const StepA
     float uu = 0.f;
     static_for<0, D>([&](auto dc) { uu += u[dc.value] * u[dc.value]; });
 
-    if (a.cap_rho && (own_flag & LBM_FLAG_CAPTURE_DENSITY)) bc_own_base[(size_t)T * D] = rho;
-    if (a.cap_u && (own_flag & LBM_FLAG_CAPTURE_VELOCITY))
+    if (active && a.cap_rho && (own_flag & LBM_FLAG_CAPTURE_DENSITY)) bc_own_base[(size_t)T * D] = rho;
+    if (active && a.cap_u && (own_flag & LBM_FLAG_CAPTURE_VELOCITY))
         static_for<0, D>([&](auto dc) { bc_own_base[(size_t)T * dc.value] = u[dc.value]; });
 
     float tau_local = tau;
@@ -208,13 +216,28 @@ __device__ __forceinline__ void collide(float (&f)[L::Q], float tau, const StepA
             // get_Smagorinsky_LES_tau (src/lbm/kernels/ops/turbulence.mojo:12-38)
             const float k = -1.f / (2.f * rho * (float)(1.0 / 3.0) * tau_local);
             float s2 = 0.f;
+            float S[L::NS];
             static_for<0, L::NS>([&](auto nc) {
                 constexpr int n = nc.value;
-                const float S = P[n] * k;
-                if constexpr (sa<L>(n) != sb<L>(n)) s2 += (S * S) * 2.f;
-                else s2 += S * S;
+                S[n] = P[n] * k;
+                if constexpr (sa<L>(n) != sb<L>(n)) s2 += (S[n] * S[n]) * 2.f;
+                else s2 += S[n] * S[n];
             });
-            tau_local += 3.f * ((a.Cs * a.Cs) * sqrtf(2.f * s2));
+            const float smag = 3.f * ((a.Cs * a.Cs) * sqrtf(2.f * s2));
+            if constexpr (LES == kLesLearned) {
+                // learned closure (every thread of the block), Smagorinsky outside the training range
+                __shared__ uint4 stage[8][32];
+                __shared__ float ys[8][32];
+                const uint32_t w = threadIdx.x >> 5;
+                float x[8];
+                closure_features<D>(S, s2, rho, uu, tau_local, x);
+                __syncthreads();  // the staged fragments are visible
+                bool in_range;
+                const float nu = warp_closure_nu(cl, x, stage[w], ys[w], in_range);
+                tau_local += in_range ? 3.f * nu : smag;
+            } else {
+                tau_local += smag;
+            }
         }
         if constexpr (COLL == LBM_RLBM) {
             // RLBM (src/lbm/kernels/ops/collisions/collision.mojo:168-223)
@@ -340,13 +363,14 @@ __device__ __forceinline__ void equilibrium_bc(float (&f)[L::Q], const float* bc
     for_each_feq<L>(rs, us, uu, ddf, [&](auto qc, float e) { f[decltype(qc)::value] = e; });
 }
 
-template <class L, int METHOD, bool F16C, int COLL, bool LES>
+template <class L, int METHOD, bool F16C, int COLL, int LES>
 __global__ void __launch_bounds__(256) step_kernel(const StepArgs a) {
     using P = Pop<F16C>;
     using S = typename P::T;
     constexpr int Q = L::Q, D = L::D, K = D + 1;
     constexpr bool ESO = METHOD == LBM_ESOTERIC_PULL;
 
+    static_assert(LES != kLesLearned, "the learned closure runs in the block-per-tile kernel");
     const uint32_t n = blockIdx.x * blockDim.x + threadIdx.x;
     if (n >= a.lay.ncells) return;
     const uint8_t flag = __ldg(a.flags + n);
@@ -471,9 +495,11 @@ __global__ void __launch_bounds__(256) step_kernel(const StepArgs a) {
 constexpr uint32_t kTileCells = 256;
 
 // The per-thread body of the block-per-tile step: thread `tid` of the CTA that owns tile `tile`.
-// Every lane of a warp must call it (it starts with a warp ballot).
-template <class L, int METHOD, bool F16C, int COLL, bool LES>
-__device__ __forceinline__ void tile_step(const StepArgs& a, const uint32_t tile, const uint32_t tid) {
+// Every lane of a warp must call it (it starts with a warp ballot); with a closure (cl, staged in
+// shared memory) every thread of the block must.
+template <class L, int METHOD, bool F16C, int COLL, int LES>
+__device__ __forceinline__ void tile_step(const StepArgs& a, const uint32_t tile, const uint32_t tid,
+                                          const ClosureDev* cl = nullptr) {
     using P = Pop<F16C>;
     using S = typename P::T;
     constexpr int Q = L::Q, D = L::D, K = D + 1;
@@ -501,10 +527,15 @@ __device__ __forceinline__ void tile_step(const StepArgs& a, const uint32_t tile
     const bool clean = __ballot_sync(0xffffffffu, special != 0u) == 0u;
 
     uint8_t flag = 0;
+    bool active = true;
     if (!clean) {
         flag = __ldg(a.flags + n);
-        // is_valid_thread (src/lbm/kernels/utils/checks.mojo:55-60)
-        if ((flag & 0x0F) == LBM_FLAG_SOLID || (flag & LBM_FLAG_EXCLUDE)) return;
+        // is_valid_thread (src/lbm/kernels/utils/checks.mojo:55-60); the learned closure keeps
+        // every thread for its block-wide staging and warp-wide products, the invalid ones write nothing
+        active = !((flag & 0x0F) == LBM_FLAG_SOLID || (flag & LBM_FLAG_EXCLUDE));
+        if constexpr (LES != kLesLearned) {
+            if (!active) return;
+        }
     }
 
     // ---- per-axis neighbour deltas, in cells (flags, bc) and in population elements (f)
@@ -598,7 +629,10 @@ __device__ __forceinline__ void tile_step(const StepArgs& a, const uint32_t tile
                               (int32_t)(by * ty + ly), (int32_t)(bz * tz + lz), a.lay, a.ddf != 0);
     }
 
-    collide<L, COLL, LES>(f, a.tau, a, a.bc + (tid + (uint64_t)T * K * tile), T, flag);
+    collide<L, COLL, LES>(f, a.tau, a, a.bc + (tid + (uint64_t)T * K * tile), T, flag, active, cl);
+    if constexpr (LES == kLesLearned) {
+        if (!active) return;
+    }
 
     // ---- store
     if constexpr (!ESO) {
@@ -619,22 +653,23 @@ __device__ __forceinline__ void tile_step(const StepArgs& a, const uint32_t tile
     }
 }
 
-template <class L, int METHOD, bool F16C, int COLL, bool LES>
-__global__ void __launch_bounds__(256, (L::Q == 9) ? 5 : ((COLL == LBM_KBC || L::Q == 27) ? 3 : 4)) step_kernel_tile(const StepArgs a) {
-    tile_step<L, METHOD, F16C, COLL, LES>(a, blockIdx.x, threadIdx.x);
+template <class L, int METHOD, bool F16C, int COLL, int LES>
+__global__ void __launch_bounds__(256, (LES == kLesLearned) ? 2 : (L::Q == 9) ? 5 : ((COLL == LBM_KBC || L::Q == 27) ? 3 : 4))
+    step_kernel_tile(const StepArgs a) {
+    tile_step<L, METHOD, F16C, COLL, LES>(a, blockIdx.x, threadIdx.x, stage_closure<LES == kLesLearned>(a.closure));
 }
 
 // Launcher type used by the dispatch tables.
 using StepLaunch = cudaError_t (*)(const StepArgs&, int threads, cudaStream_t);
 
-template <class L, int METHOD, bool F16C, int COLL, bool LES>
+template <class L, int METHOD, bool F16C, int COLL, int LES>
 cudaError_t launch_step(const StepArgs& a, int threads, cudaStream_t s) {
     const uint32_t blocks = (a.lay.ncells + (uint32_t)threads - 1u) / (uint32_t)threads;
     step_kernel<L, METHOD, F16C, COLL, LES><<<blocks, threads, 0, s>>>(a);
     return cudaGetLastError();
 }
 
-template <class L, int METHOD, bool F16C, int COLL, bool LES>
+template <class L, int METHOD, bool F16C, int COLL, int LES>
 cudaError_t launch_step_tile(const StepArgs& a, int, cudaStream_t s) {
     step_kernel_tile<L, METHOD, F16C, COLL, LES><<<a.lay.ncells / kTileCells, kTileCells, 0, s>>>(a);
     return cudaGetLastError();
@@ -650,5 +685,16 @@ cudaError_t launch_step_tile(const StepArgs& a, int, cudaStream_t s) {
      LBM_STEP_ROW(FN, L, LBM_ESOTERIC_PULL, false), LBM_STEP_ROW(FN, L, LBM_ESOTERIC_PULL, true)}
 
 inline int step_index(int method, int f16c, int coll, int les) { return ((method * 2 + f16c) * 4 + coll) * 2 + les; }
+
+// Tables of the 16 learned-closure variants of one lattice (block-per-tile kernel), indexed by
+// (method*2 + f16c)*4 + collision.
+#define LBM_LEARNED_ROW(FN, L, M, F)                                                           \
+    &FN<L, M, F, LBM_SRT, kLesLearned>, &FN<L, M, F, LBM_TRT, kLesLearned>,                  \
+        &FN<L, M, F, LBM_KBC, kLesLearned>, &FN<L, M, F, LBM_RLBM, kLesLearned>
+#define LBM_LEARNED_TABLE(FN, L)                                                               \
+    {LBM_LEARNED_ROW(FN, L, LBM_DOUBLE_BUFFER, false), LBM_LEARNED_ROW(FN, L, LBM_DOUBLE_BUFFER, true), \
+     LBM_LEARNED_ROW(FN, L, LBM_ESOTERIC_PULL, false), LBM_LEARNED_ROW(FN, L, LBM_ESOTERIC_PULL, true)}
+
+inline int learned_index(int method, int f16c, int coll) { return (method * 2 + f16c) * 4 + coll; }
 
 }  // namespace lbm

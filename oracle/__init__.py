@@ -46,6 +46,8 @@ def lib() -> C.CDLL:
         h.oracle_layout_offset.restype = i64
         h.oracle_lattice.argtypes = [i32, vp, vp, vp]
         h.oracle_max_threads.restype = i32
+        h.oracle_set_closure.argtypes = [vp]
+        h.oracle_closure_eval.argtypes = [i32, i32, i64, vp, vp, vp, vp, vp, vp, vp]
         _lib = h
     return _lib
 
@@ -146,3 +148,42 @@ def lattice(lattice_id: int):
 
 def max_threads() -> int:
     return int(lib().oracle_max_threads())
+
+
+class closure_t(C.Structure):
+    """lbm_closure_t of include/lbm_gb300.h."""
+    _fields_ = [("w1", C.c_float * 256), ("b1", C.c_float * 32), ("w2", C.c_float * 1024), ("b2", C.c_float * 32),
+                ("w3", C.c_float * 32), ("b3", C.c_float), ("nu_scale", C.c_float),
+                ("feat_mean", C.c_float * 8), ("feat_scale", C.c_float * 8), ("feat_lo", C.c_float * 8),
+                ("feat_hi", C.c_float * 8)]
+
+
+def closure_struct(theta: np.ndarray, nu_scale: float, mean, scale, lo, hi) -> closure_t:
+    """Packs the 1377 parameters (w1, b1, w2, b2, w3, b3) and the feature normalisation."""
+    t = np.asarray(theta, dtype=np.float32).ravel()
+    c = closure_t()
+    o = 0
+    for name, n in (("w1", 256), ("b1", 32), ("w2", 1024), ("b2", 32), ("w3", 32)):
+        getattr(c, name)[:] = t[o:o + n].tolist()
+        o += n
+    c.b3 = float(t[o])
+    c.nu_scale = float(nu_scale)
+    for name, v in (("feat_mean", mean), ("feat_scale", scale), ("feat_lo", lo), ("feat_hi", hi)):
+        getattr(c, name)[:] = [float(a) for a in np.asarray(v, dtype=np.float64).ravel()]
+    return c
+
+
+def set_closure(c: closure_t | None) -> None:
+    """Learned closure for the oracle's LES steps (None: Smagorinsky)."""
+    lib().oracle_set_closure(None if c is None else C.byref(c))
+
+
+def closure_eval(D: int, prec: int, S, s2, rho, uu, tau):
+    """Features (n, 8) and nu_t (n; -1 outside the training range) for explicit strain rows."""
+    S = np.ascontiguousarray(S, dtype=np.float64)
+    n = S.shape[0]
+    args = [np.ascontiguousarray(np.broadcast_to(np.asarray(a, dtype=np.float64), (n,))) for a in (s2, rho, uu, tau)]
+    x = np.zeros((n, 8), dtype=np.float64)
+    nu = np.zeros(n, dtype=np.float64)
+    lib().oracle_closure_eval(D, prec, n, _p(S), *[_p(a) for a in args], _p(x), _p(nu))
+    return x, nu

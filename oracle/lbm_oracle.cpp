@@ -165,6 +165,79 @@ inline bool flag_is(uint8_t f, uint8_t e) { return (f & 0x0F) == e; } /* Flags.i
  * The step.  R is the arithmetic type; every intermediate is rounded to R exactly where the
  * reference's Scalar[float_dtype] arithmetic rounds (compiled with -ffp-contract=off).
  * ---------------------------------------------------------------------------------------- */
+/* ---- learned subgrid closure (no counterpart in the reference; the GPU evaluates it on the
+ * tensor cores).  BF16 rounding of weights and activations is emulated, products and sums are
+ * taken in R, so the GPU matches this within the order of its FP32 accumulation. */
+bool g_closure_on = false;
+lbm_closure_t g_closure;
+
+float bf16_round(float x) {
+    uint32_t u;
+    std::memcpy(&u, &x, 4);
+    if ((u & 0x7FFFFFFFu) > 0x7F800000u) return x;
+    u += 0x7FFFu + ((u >> 16) & 1u);
+    u &= 0xFFFF0000u;
+    float r;
+    std::memcpy(&r, &u, 4);
+    return r;
+}
+
+/* Features x0..x7 of the cell (the lbm_closure_t comment in include/lbm_gb300.h lists them).
+ * S in stress order (2D xx, xy, yy; 3D xx, xy, xz, yy, yz, zz). */
+template <class R>
+void closure_features(int D, const R* S, R s2, R rho, R uu, R tau, R* x) {
+    const R snorm = std::sqrt((R)2 * s2);
+    R tr, det, off;
+    if (D == 3) {
+        tr = S[0] + S[3] + S[5];
+        const R m = tr / (R)3;
+        const R a = S[0] - m, b = S[3] - m, c = S[5] - m;
+        det = a * (b * c - S[4] * S[4]) - S[1] * (S[1] * c - S[4] * S[2]) + S[2] * (S[1] * S[4] - b * S[2]);
+        off = (R)2 * (S[1] * S[1] + S[2] * S[2] + S[4] * S[4]);
+    } else {
+        tr = S[0] + S[2];
+        const R m = tr / (R)2;
+        const R a = S[0] - m, b = S[2] - m;
+        det = a * b - S[1] * S[1];
+        off = (R)2 * (S[1] * S[1]);
+    }
+    x[0] = std::log(snorm + (R)1e-12);
+    x[1] = tr / (snorm + (R)1e-12);
+    x[2] = det / (snorm * snorm * snorm + (R)1e-30);
+    x[3] = rho - (R)1;
+    x[4] = std::sqrt(uu);
+    x[5] = off / (s2 + (R)1e-30);
+    x[6] = std::log(tau - (R)0.5);
+    x[7] = uu / (snorm + (R)1e-12);
+}
+
+/* nu_t of the learned closure, or -1 when a normalised feature leaves the training range. */
+template <class R>
+R closure_nu(const R* x) {
+    const lbm_closure_t& c = g_closure;
+    float xn[8];
+    for (int k = 0; k < 8; ++k) {
+        const float v = ((float)x[k] - c.feat_mean[k]) * c.feat_scale[k];
+        if (!(v >= c.feat_lo[k] && v <= c.feat_hi[k])) return (R)-1;
+        xn[k] = bf16_round(v);
+    }
+    R h1[32], h2[32];
+    for (int j = 0; j < 32; ++j) {
+        R a = (R)c.b1[j];
+        for (int k = 0; k < 8; ++k) a += (R)xn[k] * (R)bf16_round(c.w1[k * 32 + j]);
+        h1[j] = (R)bf16_round((float)(a > 0 ? a : 0));
+    }
+    for (int j = 0; j < 32; ++j) {
+        R a = (R)c.b2[j];
+        for (int k = 0; k < 32; ++k) a += h1[k] * (R)bf16_round(c.w2[k * 32 + j]);
+        h2[j] = (R)bf16_round((float)(a > 0 ? a : 0));
+    }
+    R y = (R)c.b3;
+    for (int k = 0; k < 32; ++k) y += h2[k] * (R)bf16_round(c.w3[k]);
+    const R sp = y > (R)20 ? y : std::log1p(std::exp(y));
+    return sp * (R)c.nu_scale;
+}
+
 template <class R, class S> struct Stepper {
     const lbm_config_t& cfg;
     const LatticeDef& L;
@@ -274,14 +347,21 @@ template <class R, class S> struct Stepper {
                 /* get_strain_rate_tensor (moment.mojo:154-176), norm (:182-215),
                  * get_Smagorinsky_LES_tau (ops/turbulence.mojo:12-38) */
                 const R k = (R)-1 / ((R)2 * rho * cs2 * tau_local);
-                R s2 = 0;
+                R s2 = 0, Sv[6];
                 for (int n = 0; n < nstress(); ++n) {
                     const R Sn = P[n] * k;
+                    Sv[n] = Sn;
                     const R ss = Sn * Sn;
                     s2 = (sa(n) != sb(n)) ? s2 + ss * (R)2 : s2 + ss;
                 }
                 const R Cs = (R)cfg.Cs;
-                const R v_eddy = (Cs * Cs) * (R)std::sqrt((R)2 * s2);
+                R v_eddy = (Cs * Cs) * (R)std::sqrt((R)2 * s2);
+                if (g_closure_on) {  /* learned closure; Smagorinsky outside the training range */
+                    R x[8];
+                    closure_features<R>(L.D, Sv, s2, rho, uu, tau_local, x);
+                    const R nu = closure_nu<R>(x);
+                    if (nu >= 0) v_eddy = nu;
+                }
                 tau_local = tau_local + (R)3 * v_eddy;
             }
             if (cfg.collision_op == LBM_RLBM) {
@@ -808,6 +888,34 @@ int oracle_lattice(int id, int32_t* c_out /* Q*3 */, double* w_out, int32_t* opp
         opp_out[q] = L.opp[q];
     }
     return L.Q;
+}
+
+/* Learned closure for the LES steps that follow (copied; NULL returns to Smagorinsky). */
+void oracle_set_closure(const lbm_closure_t* c) {
+    g_closure_on = c != nullptr;
+    if (c) g_closure = *c;
+}
+
+/* The closure's features and nu_t for explicit strain tensors: n rows of S (D=2: 3, D=3: 6
+ * components), s2, rho, uu and tau; x_out (n*8) and nu_out (n; -1 outside the training range).
+ * prec 32 or 64 as for oracle_step. */
+void oracle_closure_eval(int D, int prec, int64_t n, const double* S, const double* s2, const double* rho,
+                         const double* uu, const double* tau, double* x_out, double* nu_out) {
+    const int ns = D == 3 ? 6 : 3;
+    for (int64_t i = 0; i < n; ++i) {
+        if (prec == 64) {
+            double x[8];
+            closure_features<double>(D, S + i * ns, s2[i], rho[i], uu[i], tau[i], x);
+            for (int k = 0; k < 8; ++k) x_out[i * 8 + k] = x[k];
+            nu_out[i] = g_closure_on ? closure_nu<double>(x) : -1.0;
+        } else {
+            float Sf[6], x[8];
+            for (int k = 0; k < ns; ++k) Sf[k] = (float)S[i * ns + k];
+            closure_features<float>(D, Sf, (float)s2[i], (float)rho[i], (float)uu[i], (float)tau[i], x);
+            for (int k = 0; k < 8; ++k) x_out[i * 8 + k] = x[k];
+            nu_out[i] = g_closure_on ? (double)closure_nu<float>(x) : -1.0;
+        }
+    }
 }
 
 int oracle_max_threads(void) {
