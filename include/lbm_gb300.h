@@ -255,12 +255,13 @@ int64_t lbm_batch_cells(const lbm_batch* b);
  * normalised features leave [feat_lo, feat_hi] (the training range) keep Smagorinsky.  Inference
  * runs inside the collision of LES configurations on the tensor cores (BF16 weights and
  * activations, FP32 accumulation).  Features, with S the strain rate from the non-equilibrium
- * stress (moment.mojo:154-176), s2 its squared norm (off-diagonals twice), |S| = sqrt(2 s2):
- *   x0 log(|S| + 1e-12)          x1 tr(S) / (|S| + 1e-12)
- *   x2 det(S_dev) / (|S|^3 + 1e-30)   x3 rho - 1
- *   x4 |u|                       x5 2 (Sxy^2 + Sxz^2 + Syz^2) / (s2 + 1e-30)
- *   x6 log(tau - 0.5)            x7 |u|^2 / (|S| + 1e-12)
- * normalised as (x - feat_mean) * feat_scale.  Weights are stored input-major:
+ * stress (moment.mojo:154-176), s2 its squared norm (off-diagonals twice), q = 2 s2 + 1e-24:
+ *   x0 ln(q) / 2                 x1 tr(S) / sqrt(q)
+ *   x2 det(S - tr(S)/D I) / q^(3/2)   x3 rho - 1
+ *   x4 |u|                       x5 2 (Sxy^2 + Sxz^2 + Syz^2) / s2 (as 4 (...) / q)
+ *   x6 ln(tau - 0.5)             x7 |u|^2 / sqrt(q)
+ * (the kernel evaluates them with approximate rsqrt, sqrt and log2), normalised as
+ * fma(x, feat_scale, -feat_mean * feat_scale).  Weights are stored input-major:
  * w1[k*32 + j] links input k to hidden unit j, w2[k*32 + j] likewise, w3[k] hidden k to y. */
 typedef struct lbm_closure_t {
     float w1[8 * 32];

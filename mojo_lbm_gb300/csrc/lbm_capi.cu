@@ -22,7 +22,7 @@ StepLaunch get_tile_step_d3q27(int, int, int, int);
 StepLaunch get_learned_step_d2q9(int, int, int);
 StepLaunch get_learned_step_d3q19(int, int, int);
 StepLaunch get_learned_step_d3q27(int, int, int);
-void pack_closure(const lbm_closure_t& c, ClosureDev& d);
+void pack_closure(const lbm_closure_t& c, ClosureDev& d, ClosureUniform& u);
 }  // namespace lbm
 
 using namespace lbm;
@@ -85,6 +85,7 @@ struct lbm_handle {
     int sm_count;
     double* scratch;  // kReduceBlocks*4 partials + 4 results
     ClosureDev* closure;  // device copy of the learned closure's fragments, or null
+    ClosureUniform closure_uniform;
     int closure_on;
     cudaStream_t capture_stream;
     std::map<GraphKey, cudaGraphExec_t> graphs;
@@ -125,6 +126,7 @@ StepArgs step_args(const lbm_handle* h, const void* f_in, void* f_out, float* bc
     a.cap_u = h->cfg.capture_velocity;
     a.even = even;
     a.closure = h->closure_on ? h->closure : nullptr;
+    a.cl = h->closure_uniform;
     a.tile_any = h->tile_any;
     a.mx = h->mx;
     a.my = h->my;
@@ -277,6 +279,7 @@ lbm_status lbm_create(const lbm_config_t* cfg, const lbm_grid_t* grid, lbm_handl
     h->threads = 256;
     h->scratch = nullptr;
     h->closure = nullptr;
+    std::memset(&h->closure_uniform, 0, sizeof(h->closure_uniform));
     h->closure_on = 0;
     h->capture_stream = nullptr;
     cudaError_t e = cudaGetDevice(&h->device);
@@ -325,7 +328,7 @@ lbm_status lbm_set_closure(lbm_handle* h, const lbm_closure_t* closure) {
         return LBM_OK;
     }
     ClosureDev d;
-    pack_closure(*closure, d);
+    pack_closure(*closure, d, h->closure_uniform);
     if (!h->closure) LBM_CK(cudaMalloc(&h->closure, sizeof(ClosureDev)));
     LBM_CK(cudaMemcpy(h->closure, &d, sizeof(ClosureDev), cudaMemcpyHostToDevice));
     h->closure_on = 1;

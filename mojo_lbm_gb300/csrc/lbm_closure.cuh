@@ -18,29 +18,29 @@ namespace lbm {
 
 struct alignas(16) ClosureDev {
     uint2 w1f[4][32];      // [n-tile][lane]: B fragment of W1 (K = 8 features, zero-padded to 16)
-    uint2 w2f[4][2][32];   // [n-tile][k-slice][lane]
-    uint2 w3f[2][32];      // [k-slice][lane] (output column 0 only)
-    float2 b1f[4][32];     // [n-tile][lane]: biases of the lane's two accumulator columns
-    float2 b2f[4][32];
-    float mean[8], scale[8], lo[8], hi[8];
-    float b3, nu_scale, pad_[2];
+    uint4 w2f[4][32];      // [n-tile][lane]: B fragments of W2, k-slice 0 in .x .y, k-slice 1 in .z .w
+    uint4 w3f[32];         // [lane]: B fragments of w3 (output column 0 only), k-slices as W2's
+    float4 b1q[4][32];     // [n-tile][lane]: biases of the lane's two accumulator columns laid out as
+    float4 b2q[4][32];     // the accumulator quad (c0 c1 | c2 c3 = rows g | g+8): the MMA's C input
+    float4 b3q;            // output bias, same layout
+};
+
+// The warp-uniform part of the closure, passed by value with the step's arguments (kernel
+// parameter space: read as instruction operands, no loads).
+struct ClosureUniform {
+    float scale[8], shift[8], lo[8], hi[8];  // x_n = fma(x, scale, shift), shift = -mean * scale
+    float nu_scale;
 };
 static_assert(sizeof(ClosureDev) % 16 == 0, "ClosureDev is copied in 16-byte words");
 
 // Copies the closure's fragments into this CTA's shared memory (every thread of the block takes
-// part; the caller synchronises the block before the first use).  Null stays null.
-template <bool LES>
+// part; the caller synchronises the block before the first use).
 __device__ __forceinline__ const ClosureDev* stage_closure(const ClosureDev* g) {
-    if constexpr (!LES) {
-        return nullptr;
-    } else {
-        __shared__ ClosureDev s;
-        if (g == nullptr) return nullptr;
-        const uint4* src = reinterpret_cast<const uint4*>(g);
-        uint4* dst = reinterpret_cast<uint4*>(&s);
-        for (uint32_t i = threadIdx.x; i < sizeof(ClosureDev) / 16; i += blockDim.x) dst[i] = __ldg(src + i);
-        return &s;
-    }
+    __shared__ ClosureDev s;
+    const uint4* src = reinterpret_cast<const uint4*>(g);
+    uint4* dst = reinterpret_cast<uint4*>(&s);
+    for (uint32_t i = threadIdx.x; i < sizeof(ClosureDev) / 16; i += blockDim.x) dst[i] = __ldg(src + i);
+    return &s;
 }
 
 __device__ __forceinline__ uint32_t pack_bf16x2(float lo, float hi) {
@@ -48,6 +48,42 @@ __device__ __forceinline__ uint32_t pack_bf16x2(float lo, float hi) {
     return *reinterpret_cast<const uint32_t*>(&v);
 }
 
+// ReLU and BF16 rounding of two accumulators in one instruction (lo in the low half).
+__device__ __forceinline__ uint32_t relu_bf16x2(float lo, float hi) {
+    uint32_t r;
+    asm("cvt.rn.relu.bf16x2.f32 %0, %1, %2;" : "=r"(r) : "f"(hi), "f"(lo));
+    return r;
+}
+
+__device__ __forceinline__ void sts128(float4* p, float a, float b, float c, float d) {
+    const uint32_t addr = (uint32_t)__cvta_generic_to_shared(p);
+    asm volatile("st.shared.v4.f32 [%0], {%1, %2, %3, %4};" ::"r"(addr), "f"(a), "f"(b), "f"(c), "f"(d) : "memory");
+}
+__device__ __forceinline__ float4 lds128(const float4* p) {
+    const uint32_t addr = (uint32_t)__cvta_generic_to_shared(p);
+    float4 v;
+    asm volatile("ld.shared.v4.f32 {%0, %1, %2, %3}, [%4];" : "=f"(v.x), "=f"(v.y), "=f"(v.z), "=f"(v.w) : "r"(addr)
+                 : "memory");
+    return v;
+}
+
+__device__ __forceinline__ float rsqrt_approx(float x) {
+    float r;
+    asm("rsqrt.approx.f32 %0, %1;" : "=f"(r) : "f"(x));
+    return r;
+}
+__device__ __forceinline__ float sqrt_approx(float x) {
+    float r;
+    asm("sqrt.approx.f32 %0, %1;" : "=f"(r) : "f"(x));
+    return r;
+}
+__device__ __forceinline__ float lg2_approx(float x) {
+    float r;
+    asm("lg2.approx.f32 %0, %1;" : "=f"(r) : "f"(x));
+    return r;
+}
+
+// d = a b + d
 __device__ __forceinline__ void mma_bf16_16816(float (&d)[4], const uint32_t (&a)[4], uint2 b) {
     asm volatile(
         "mma.sync.aligned.m16n8k16.row.col.f32.bf16.bf16.f32 {%0,%1,%2,%3}, {%4,%5,%6,%7}, {%8,%9}, "
@@ -56,103 +92,172 @@ __device__ __forceinline__ void mma_bf16_16816(float (&d)[4], const uint32_t (&a
         : "r"(a[0]), "r"(a[1]), "r"(a[2]), "r"(a[3]), "r"(b.x), "r"(b.y));
 }
 
-// The eight closure features of a cell (see lbm_closure_t in the C header).  S: strain-rate
-// components in stress order (2D xx, xy, yy; 3D xx, xy, xz, yy, yz, zz), s2 its squared norm.
+// d = a b + c: c is the bias quad (loaded as one 128-bit word, used as is)
+__device__ __forceinline__ void mma_bf16_16816_bias(float (&d)[4], const uint32_t (&a)[4], uint2 b, float4 c) {
+    asm volatile(
+        "mma.sync.aligned.m16n8k16.row.col.f32.bf16.bf16.f32 {%0,%1,%2,%3}, {%4,%5,%6,%7}, {%8,%9}, "
+        "{%10,%11,%12,%13};\n"
+        : "=f"(d[0]), "=f"(d[1]), "=f"(d[2]), "=f"(d[3])
+        : "r"(a[0]), "r"(a[1]), "r"(a[2]), "r"(a[3]), "r"(b.x), "r"(b.y), "f"(c.x), "f"(c.y), "f"(c.z), "f"(c.w));
+}
+
+// The eight closure features of a cell (definitions in the lbm_closure_t comment of the C
+// header), with the hardware's approximate rsqrt / sqrt / log2: network inputs need no IEEE
+// rounding.  S: strain-rate components in stress order (2D xx, xy, yy; 3D xx, xy, xz, yy, yz,
+// zz), s2 its squared norm (off-diagonals twice).
 template <int D>
 __device__ __forceinline__ void closure_features(const float* S, float s2, float rho, float uu, float tau,
                                                  float (&x)[8]) {
-    const float snorm = sqrtf(2.f * s2);
     float tr, det, off;
     if constexpr (D == 3) {
         tr = S[0] + S[3] + S[5];
         const float m = tr * (1.f / 3.f);
         const float a = S[0] - m, b = S[3] - m, c = S[5] - m;
-        det = a * (b * c - S[4] * S[4]) - S[1] * (S[1] * c - S[4] * S[2]) + S[2] * (S[1] * S[4] - b * S[2]);
-        off = 2.f * (S[1] * S[1] + S[2] * S[2] + S[4] * S[4]);
+        const float t1 = __fmaf_rn(b, c, -(S[4] * S[4]));
+        const float t2 = __fmaf_rn(-S[4], S[2], S[1] * c);
+        const float t3 = __fmaf_rn(-b, S[2], S[1] * S[4]);
+        det = __fmaf_rn(S[2], t3, __fmaf_rn(-S[1], t2, a * t1));
+        off = 2.f * __fmaf_rn(S[4], S[4], __fmaf_rn(S[2], S[2], S[1] * S[1]));
     } else {
         tr = S[0] + S[2];
         const float m = tr * 0.5f;
         const float a = S[0] - m, b = S[2] - m;
-        det = a * b - S[1] * S[1];
+        det = __fmaf_rn(a, b, -(S[1] * S[1]));
         off = 2.f * (S[1] * S[1]);
     }
-    // network inputs need no IEEE rounding: fast log and division (the oracle uses libm's)
-    const float inv_s = __fdividef(1.f, snorm + 1e-12f);
-    x[0] = __logf(snorm + 1e-12f);
-    x[1] = tr * inv_s;
-    x[2] = __fdividef(det, snorm * snorm * snorm + 1e-30f);
+    const float q = __fmaf_rn(2.f, s2, 1e-24f);  // |S|^2 (+ floor)
+    const float r = rsqrt_approx(q);    // 1 / |S|
+    constexpr float half_ln2 = 0.34657359027997264f;
+    constexpr float ln2 = 0.69314718055994531f;
+    x[0] = lg2_approx(q) * half_ln2;
+    x[1] = tr * r;
+    x[2] = det * (r * r * r);
     x[3] = rho - 1.f;
-    x[4] = sqrtf(uu);
-    x[5] = __fdividef(off, s2 + 1e-30f);
-    x[6] = __logf(tau - 0.5f);
-    x[7] = uu * inv_s;
+    x[4] = sqrt_approx(uu);
+    x[5] = off * (2.f * (r * r));
+    x[6] = lg2_approx(tau - 0.5f) * ln2;
+    x[7] = uu * r;
 }
 
-// nu_t of the calling lane's cell; every lane of the warp must call it.  stage: 32 x uint4 of
-// per-warp shared memory, ys: 32 floats of per-warp shared memory.  in_range reports whether the
-// normalised features lie in the training range.
-__device__ __forceinline__ float warp_closure_nu(const ClosureDev* __restrict__ c, const float (&x)[8], uint4* stage,
-                                                 float* ys, bool& in_range) {
+#ifndef LBM_CLOSURE_INTERLEAVE
+#define LBM_CLOSURE_INTERLEAVE 1
+#endif
+
+// Next layer's A fragments from a layer's accumulators: the accumulator layout of m16n8k16 (rows
+// g, g+8; columns 2t, 2t+1) is the A layout of the next k-slice, n-tiles 2kc and 2kc+1 forming
+// k-slice kc.  ReLU and BF16 rounding in one instruction per pair.
+__device__ __forceinline__ void relu_to_a(const float (&h)[4][4], uint32_t (&a)[2][4]) {
+#pragma unroll
+    for (int kc = 0; kc < 2; ++kc) {
+        a[kc][0] = relu_bf16x2(h[2 * kc][0], h[2 * kc][1]);
+        a[kc][1] = relu_bf16x2(h[2 * kc][2], h[2 * kc][3]);
+        a[kc][2] = relu_bf16x2(h[2 * kc + 1][0], h[2 * kc + 1][1]);
+        a[kc][3] = relu_bf16x2(h[2 * kc + 1][2], h[2 * kc + 1][3]);
+    }
+}
+
+// nu_t of the calling lane's cell; every lane of the warp must call it.  c: the per-lane
+// fragments in shared memory; u: the uniform part; stage: 32 x uint4 of per-warp shared memory,
+// ys: 32 floats of per-warp shared memory.  in_range reports whether the normalised features
+// lie in the training range (finite weights assumed: lbm_set_closure rejects others).  With LBM_CLOSURE_INTERLEAVE both 16-cell row tiles of the warp go
+// through each layer together (every weight fragment read once, used twice); without, one row
+// tile after the other (fewer live registers).
+__device__ __forceinline__ float warp_closure_nu(const ClosureDev* __restrict__ c, const ClosureUniform& u,
+                                                 const float (&x)[8], uint4* stage, float* ys, bool& in_range) {
     const uint32_t lane = threadIdx.x & 31u, g = lane >> 2, t = lane & 3u;
     float xn[8];
-    in_range = true;
+    bool ok = true;
 #pragma unroll
     for (int k = 0; k < 8; ++k) {
-        xn[k] = (x[k] - c->mean[k]) * c->scale[k];
-        in_range = in_range && xn[k] >= c->lo[k] && xn[k] <= c->hi[k];
+        xn[k] = __fmaf_rn(x[k], u.scale[k], u.shift[k]);
+        ok = ok & (xn[k] >= u.lo[k]) & (xn[k] <= u.hi[k]);  // no short circuit: predicate chain
     }
+    // The verdict rides in the data: a cell outside the training range enters the network as NaN,
+    // which stays in its own row of every product, and leaves it as NaN (nothing else stays live
+    // across the network).
+    xn[0] = ok ? xn[0] : __int_as_float(0x7FC00000);
     stage[lane] = make_uint4(pack_bf16x2(xn[0], xn[1]), pack_bf16x2(xn[2], xn[3]), pack_bf16x2(xn[4], xn[5]),
                              pack_bf16x2(xn[6], xn[7]));
     __syncwarp();
     const uint32_t* st = reinterpret_cast<const uint32_t*>(stage);
+#if LBM_CLOSURE_INTERLEAVE
+    // layer 1: rows = cells 16 mt + g (+8), columns = features 2t, 2t+1 (K padded to 16)
+    uint32_t a[2][2][4];  // [mt][k-slice]
 #pragma unroll
     for (int mt = 0; mt < 2; ++mt) {
-        // layer 1: rows = cells 16 mt + g (+8), columns = features 2t, 2t+1 (K padded to 16)
-        const uint32_t a1[4] = {st[(16 * mt + g) * 4 + t], st[(16 * mt + g + 8) * 4 + t], 0u, 0u};
-        float h1[4][4];
+        a[mt][0][0] = st[(16 * mt + g) * 4 + t];
+        a[mt][0][1] = st[(16 * mt + g + 8) * 4 + t];
+        a[mt][0][2] = a[mt][0][3] = 0u;
+    }
+    float h[2][4][4];  // [mt][n-tile][accumulator]
 #pragma unroll
-        for (int nt = 0; nt < 4; ++nt) {
-            const float2 bb = c->b1f[nt][lane];
-            h1[nt][0] = bb.x; h1[nt][1] = bb.y; h1[nt][2] = bb.x; h1[nt][3] = bb.y;
-            mma_bf16_16816(h1[nt], a1, c->w1f[nt][lane]);
+    for (int nt = 0; nt < 4; ++nt) {
+        const float4 bb = c->b1q[nt][lane];
+        const uint2 w = c->w1f[nt][lane];
+#pragma unroll
+        for (int mt = 0; mt < 2; ++mt) mma_bf16_16816_bias(h[mt][nt], a[mt][0], w, bb);
+    }
+#pragma unroll
+    for (int mt = 0; mt < 2; ++mt) relu_to_a(h[mt], a[mt]);
+#pragma unroll
+    for (int nt = 0; nt < 4; ++nt) {  // layer 2
+        const float4 bb = c->b2q[nt][lane];
+        const uint4 ww = c->w2f[nt][lane];
+        const uint2 w0 = make_uint2(ww.x, ww.y), w1 = make_uint2(ww.z, ww.w);
+#pragma unroll
+        for (int mt = 0; mt < 2; ++mt) {
+            mma_bf16_16816_bias(h[mt][nt], a[mt][0], w0, bb);
+            mma_bf16_16816(h[mt][nt], a[mt][1], w1);
         }
-        uint32_t a2[2][4];
+    }
 #pragma unroll
-        for (int kc = 0; kc < 2; ++kc) {
-            a2[kc][0] = pack_bf16x2(fmaxf(h1[2 * kc][0], 0.f), fmaxf(h1[2 * kc][1], 0.f));
-            a2[kc][1] = pack_bf16x2(fmaxf(h1[2 * kc][2], 0.f), fmaxf(h1[2 * kc][3], 0.f));
-            a2[kc][2] = pack_bf16x2(fmaxf(h1[2 * kc + 1][0], 0.f), fmaxf(h1[2 * kc + 1][1], 0.f));
-            a2[kc][3] = pack_bf16x2(fmaxf(h1[2 * kc + 1][2], 0.f), fmaxf(h1[2 * kc + 1][3], 0.f));
-        }
-        float h2[4][4];
+    for (int mt = 0; mt < 2; ++mt) relu_to_a(h[mt], a[mt]);
+    const uint4 w3 = c->w3f[lane];  // layer 3 (output column 0)
+    const uint2 w30 = make_uint2(w3.x, w3.y), w31 = make_uint2(w3.z, w3.w);
 #pragma unroll
-        for (int nt = 0; nt < 4; ++nt) {
-            const float2 bb = c->b2f[nt][lane];
-            h2[nt][0] = bb.x; h2[nt][1] = bb.y; h2[nt][2] = bb.x; h2[nt][3] = bb.y;
-#pragma unroll
-            for (int kc = 0; kc < 2; ++kc) mma_bf16_16816(h2[nt], a2[kc], c->w2f[nt][kc][lane]);
-        }
-        uint32_t a3[2][4];
-#pragma unroll
-        for (int kc = 0; kc < 2; ++kc) {
-            a3[kc][0] = pack_bf16x2(fmaxf(h2[2 * kc][0], 0.f), fmaxf(h2[2 * kc][1], 0.f));
-            a3[kc][1] = pack_bf16x2(fmaxf(h2[2 * kc][2], 0.f), fmaxf(h2[2 * kc][3], 0.f));
-            a3[kc][2] = pack_bf16x2(fmaxf(h2[2 * kc + 1][0], 0.f), fmaxf(h2[2 * kc + 1][1], 0.f));
-            a3[kc][3] = pack_bf16x2(fmaxf(h2[2 * kc + 1][2], 0.f), fmaxf(h2[2 * kc + 1][3], 0.f));
-        }
-        float y[4] = {c->b3, c->b3, c->b3, c->b3};
-#pragma unroll
-        for (int kc = 0; kc < 2; ++kc) mma_bf16_16816(y, a3[kc], c->w3f[kc][lane]);
-        if (t == 0u) {  // output column 0: rows g and g + 8 of this tile
+    for (int mt = 0; mt < 2; ++mt) {
+        float y[4];
+        mma_bf16_16816_bias(y, a[mt][0], w30, c->b3q);
+        mma_bf16_16816(y, a[mt][1], w31);
+        if (t == 0u) {  // rows g and g + 8 of this tile
             ys[16 * mt + g] = y[0];
             ys[16 * mt + g + 8] = y[2];
         }
     }
+#else
+#pragma unroll 1
+    for (int mt = 0; mt < 2; ++mt) {
+        uint32_t a[2][4];
+        a[0][0] = st[(16 * mt + g) * 4 + t];
+        a[0][1] = st[(16 * mt + g + 8) * 4 + t];
+        a[0][2] = a[0][3] = 0u;
+        float h[4][4];
+#pragma unroll
+        for (int nt = 0; nt < 4; ++nt) mma_bf16_16816_bias(h[nt], a[0], c->w1f[nt][lane], c->b1q[nt][lane]);
+        relu_to_a(h, a);
+#pragma unroll
+        for (int nt = 0; nt < 4; ++nt) {
+            const uint4 ww = c->w2f[nt][lane];
+            mma_bf16_16816_bias(h[nt], a[0], make_uint2(ww.x, ww.y), c->b2q[nt][lane]);
+            mma_bf16_16816(h[nt], a[1], make_uint2(ww.z, ww.w));
+        }
+        relu_to_a(h, a);
+        float y[4];
+        const uint4 w3 = c->w3f[lane];
+        mma_bf16_16816_bias(y, a[0], make_uint2(w3.x, w3.y), c->b3q);
+        mma_bf16_16816(y, a[1], make_uint2(w3.z, w3.w));
+        if (t == 0u) {
+            ys[16 * mt + g] = y[0];
+            ys[16 * mt + g + 8] = y[2];
+        }
+    }
+#endif
     __syncwarp();
     const float yo = ys[lane];
     __syncwarp();  // stage / ys are reused by the next call
+    in_range = yo == yo;
     const float sp = yo > 20.f ? yo : __logf(1.f + __expf(yo));  // softplus
-    return sp * c->nu_scale;
+    return sp * u.nu_scale;
 }
 
 }  // namespace lbm

@@ -1,9 +1,9 @@
-// The 16 learned-closure LES variants of the D3Q19 lattice (block-per-tile kernel).
+// The 16 learned-closure LES variants of the D3Q19 lattice (persistent block-per-tile kernel).
 #include "lbm_step.cuh"
 
 namespace lbm {
 StepLaunch get_learned_step_d3q19(int method, int f16c, int coll) {
-    static const StepLaunch t[16] = LBM_LEARNED_TABLE(launch_step_tile, D3Q19);
+    static const StepLaunch t[16] = LBM_LEARNED_TABLE(launch_step_learned, D3Q19);
     return t[learned_index(method, f16c, coll)];
 }
 }  // namespace lbm

@@ -232,8 +232,9 @@ int sm_count() {
 
 // Fills the per-lane fragments of m16n8k16 B operands (k rows 2t, 2t+1 in register 0 and
 // 2t+8, 2t+9 in register 1 of column g, lane = 4g + t) and the accumulator bias pairs.
-__attribute__((visibility("hidden"))) void pack_closure(const lbm_closure_t& c, ClosureDev& d) {
+__attribute__((visibility("hidden"))) void pack_closure(const lbm_closure_t& c, ClosureDev& d, ClosureUniform& u) {
     std::memset(&d, 0, sizeof(d));
+    std::memset(&u, 0, sizeof(u));
     for (int lane = 0; lane < 32; ++lane) {
         const int g = lane >> 2, t = lane & 3;
         for (int nt = 0; nt < 4; ++nt) {
@@ -242,28 +243,33 @@ __attribute__((visibility("hidden"))) void pack_closure(const lbm_closure_t& c, 
             d.w1f[nt][lane].y = 0u;  // features 8..15 are the zero padding of K
             for (int kc = 0; kc < 2; ++kc) {
                 const int k = 16 * kc + 2 * t;
-                d.w2f[nt][kc][lane].x = pair(c.w2[k * kHid + col], c.w2[(k + 1) * kHid + col]);
-                d.w2f[nt][kc][lane].y = pair(c.w2[(k + 8) * kHid + col], c.w2[(k + 9) * kHid + col]);
+                const uint32_t r0 = pair(c.w2[k * kHid + col], c.w2[(k + 1) * kHid + col]);
+                const uint32_t r1 = pair(c.w2[(k + 8) * kHid + col], c.w2[(k + 9) * kHid + col]);
+                if (kc == 0) { d.w2f[nt][lane].x = r0; d.w2f[nt][lane].y = r1; }
+                else { d.w2f[nt][lane].z = r0; d.w2f[nt][lane].w = r1; }
             }
-            d.b1f[nt][lane] = make_float2(c.b1[8 * nt + 2 * t], c.b1[8 * nt + 2 * t + 1]);
-            d.b2f[nt][lane] = make_float2(c.b2[8 * nt + 2 * t], c.b2[8 * nt + 2 * t + 1]);
+            const float b1x = c.b1[8 * nt + 2 * t], b1y = c.b1[8 * nt + 2 * t + 1];
+            const float b2x = c.b2[8 * nt + 2 * t], b2y = c.b2[8 * nt + 2 * t + 1];
+            d.b1q[nt][lane] = make_float4(b1x, b1y, b1x, b1y);
+            d.b2q[nt][lane] = make_float4(b2x, b2y, b2x, b2y);
         }
         for (int kc = 0; kc < 2; ++kc) {
             const int k = 16 * kc + 2 * t;
             if (g == 0) {  // only output column 0 is used
-                d.w3f[kc][lane].x = pair(c.w3[k], c.w3[k + 1]);
-                d.w3f[kc][lane].y = pair(c.w3[k + 8], c.w3[k + 9]);
+                const uint32_t r0 = pair(c.w3[k], c.w3[k + 1]), r1 = pair(c.w3[k + 8], c.w3[k + 9]);
+                if (kc == 0) { d.w3f[lane].x = r0; d.w3f[lane].y = r1; }
+                else { d.w3f[lane].z = r0; d.w3f[lane].w = r1; }
             }
         }
     }
     for (int k = 0; k < 8; ++k) {
-        d.mean[k] = c.feat_mean[k];
-        d.scale[k] = c.feat_scale[k];
-        d.lo[k] = c.feat_lo[k];
-        d.hi[k] = c.feat_hi[k];
+        u.scale[k] = c.feat_scale[k];
+        u.shift[k] = -(c.feat_mean[k] * c.feat_scale[k]);  // x_n = fma(x, scale, shift)
+        u.lo[k] = c.feat_lo[k];
+        u.hi[k] = c.feat_hi[k];
     }
-    d.b3 = c.b3;
-    d.nu_scale = c.nu_scale;
+    d.b3q = make_float4(c.b3, c.b3, c.b3, c.b3);
+    u.nu_scale = c.nu_scale;
 }
 
 }  // namespace lbm

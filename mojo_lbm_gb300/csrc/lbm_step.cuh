@@ -21,6 +21,7 @@ namespace lbm {
 // LES template argument of the step kernels.
 constexpr int kLesOff = 0, kLesSmagorinsky = 1, kLesLearned = 2;
 
+
 struct StepArgs {
     LayoutDesc lay;
     const void* f_in;
@@ -30,7 +31,8 @@ struct StepArgs {
     float tau, Cs, trt_lambda;
     int32_t ddf, moving, eqbc, cap_rho, cap_u, even;
     // block-per-tile path (256-cell tiles with power-of-two sides)
-    const ClosureDev* closure; // learned LES closure, or null for Smagorinsky
+    const ClosureDev* closure; // learned LES closure's fragments (learned-closure kernels only)
+    ClosureUniform cl;         // and its warp-uniform part
     const uint8_t* tile_any;   // per tile: 1 if any flag of the tile is not FLUID (0)
     uint32_t mx, my, shx, shxy; // lx = t & mx, ly = (t >> shx) & my, lz = t >> shxy
 };
@@ -166,12 +168,15 @@ __device__ __forceinline__ float kbc_shear(const float* P) {
 }
 
 // collide (src/lbm/kernels/steps/collide.mojo:23-90).  LES: 0 off, kLesSmagorinsky, or
-// kLesLearned (the closure `cl` in shared memory, evaluated by every thread of the block; `active`
-// is false for the lanes kept alive only for it, which write nothing).
+// kLesLearned: the closure `cl` in shared memory, evaluated by every lane of the warp (`active`
+// is false for the lanes kept alive only for it, which write nothing); the populations wait in
+// `stash` (this warp's (Q+3)/4 x 32 float4 of shared memory, lane-fastest) across the features
+// and the network, and `stash_holds_f` says the stash already holds them.
 template <class L, int COLL, int LES>
 __device__ __forceinline__ void collide(float (&f)[L::Q], float tau, const StepArgs& a, float* bc_own_base,
                                         uint32_t T, uint8_t own_flag, bool active = true,
-                                        const ClosureDev* cl = nullptr) {
+                                        const ClosureDev* cl = nullptr, float4* stash = nullptr,
+                                        bool stash_holds_f = false) {
     constexpr int Q = L::Q, D = L::D;
     const bool ddf = a.ddf != 0;
     float rho = 0.f;
@@ -198,19 +203,54 @@ __device__ __forceinline__ void collide(float (&f)[L::Q], float tau, const StepA
     float tau_local = tau;
     constexpr bool NEED_NEQ = LES || COLL == LBM_KBC || COLL == LBM_RLBM;
     if constexpr (NEED_NEQ) {
-        // get_non_eq_second_order_moment (src/lbm/kernels/utils/moment.mojo:111-150)
         float P[L::NS];
         static_for<0, L::NS>([&](auto nc) { P[nc.value] = 0.f; });
-        for_each_feq<L>(rho, u, uu, ddf, [&](auto qc, float e) {
-            constexpr int q = decltype(qc)::value;
-            const float fn = f[q] - e;
-            static_for<0, L::NS>([&](auto nc) {
-                constexpr int n = nc.value;
-                constexpr int cc = L::c(q, sa<L>(n)) * L::c(q, sb<L>(n));
-                if constexpr (cc > 0) P[n] += fn;
-                else if constexpr (cc < 0) P[n] -= fn;
+        if constexpr (LES != kLesLearned) {
+            // get_non_eq_second_order_moment (src/lbm/kernels/utils/moment.mojo:111-150)
+            for_each_feq<L>(rho, u, uu, ddf, [&](auto qc, float e) {
+                constexpr int q = decltype(qc)::value;
+                const float fn = f[q] - e;
+                static_for<0, L::NS>([&](auto nc) {
+                    constexpr int n = nc.value;
+                    constexpr int cc = L::c(q, sa<L>(n)) * L::c(q, sb<L>(n));
+                    if constexpr (cc > 0) P[n] += fn;
+                    else if constexpr (cc < 0) P[n] -= fn;
+                });
             });
-        });
+        } else {
+            // The same moment from the raw second moment of f less the equilibrium's, which is
+            // rho u_a u_b + cs^2 rho delta_ab on these lattices (cs^2 (rho - 1) delta_ab for the
+            // DDF-shifted populations): algebraically equal, without f_eq per direction.  The
+            // learned-closure kernels are held to a tolerance, not to bit parity.
+            static_for<0, Q>([&](auto qc) {
+                constexpr int q = qc.value;
+                static_for<0, L::NS>([&](auto nc) {
+                    constexpr int n = nc.value;
+                    constexpr int cc = L::c(q, sa<L>(n)) * L::c(q, sb<L>(n));
+                    if constexpr (cc > 0) P[n] += f[q];
+                    else if constexpr (cc < 0) P[n] -= f[q];
+                });
+            });
+            const float rho_cs2 = (ddf ? rho - 1.f : rho) * (float)(1.0 / 3.0);
+            static_for<0, L::NS>([&](auto nc) {
+                constexpr int n = nc.value, A = sa<L>(n), B = sb<L>(n);
+                P[n] = __fmaf_rn(-rho * u[A], u[B], P[n]);
+                if constexpr (A == B) P[n] -= rho_cs2;
+            });
+        }
+        constexpr int NW = (Q + 3) / 4;
+        if constexpr (LES == kLesLearned) {
+            // 128-bit words, lane-fastest (conflict-free); explicit shared-memory instructions, so
+            // the values leave the registers
+            if (!stash_holds_f) {
+                const uint32_t lane = threadIdx.x & 31u;
+                static_for<0, NW>([&](auto jc) {
+                    constexpr int j = jc.value;
+                    sts128(stash + j * 32 + lane, f[4 * j], 4 * j + 1 < Q ? f[(4 * j + 1) % Q] : 0.f,
+                           4 * j + 2 < Q ? f[(4 * j + 2) % Q] : 0.f, 4 * j + 3 < Q ? f[(4 * j + 3) % Q] : 0.f);
+                });
+            }
+        }
         if constexpr (LES) {
             // get_strain_rate_tensor / _norm_squared (moment.mojo:154-215),
             // get_Smagorinsky_LES_tau (src/lbm/kernels/ops/turbulence.mojo:12-38)
@@ -223,21 +263,31 @@ __device__ __forceinline__ void collide(float (&f)[L::Q], float tau, const StepA
                 if constexpr (sa<L>(n) != sb<L>(n)) s2 += (S[n] * S[n]) * 2.f;
                 else s2 += S[n] * S[n];
             });
-            const float smag = 3.f * ((a.Cs * a.Cs) * sqrtf(2.f * s2));
             if constexpr (LES == kLesLearned) {
-                // learned closure (every thread of the block), Smagorinsky outside the training range
+                // learned closure (every lane of the warp), Smagorinsky outside the training range
                 __shared__ uint4 stage[8][32];
                 __shared__ float ys[8][32];
                 const uint32_t w = threadIdx.x >> 5;
                 float x[8];
                 closure_features<D>(S, s2, rho, uu, tau_local, x);
-                __syncthreads();  // the staged fragments are visible
                 bool in_range;
-                const float nu = warp_closure_nu(cl, x, stage[w], ys[w], in_range);
-                tau_local += in_range ? 3.f * nu : smag;
+                const float nu = warp_closure_nu(cl, a.cl, x, stage[w], ys[w], in_range);
+                if (in_range) tau_local += 3.f * nu;
+                else tau_local += 3.f * ((a.Cs * a.Cs) * sqrtf(2.f * s2));  // Smagorinsky (rare)
             } else {
-                tau_local += smag;
+                tau_local += 3.f * ((a.Cs * a.Cs) * sqrtf(2.f * s2));
             }
+        }
+        if constexpr (LES == kLesLearned) {
+            const uint32_t lane = threadIdx.x & 31u;
+            static_for<0, NW>([&](auto jc) {
+                constexpr int j = jc.value;
+                const float4 v = lds128(stash + j * 32 + lane);
+                f[4 * j] = v.x;
+                if constexpr (4 * j + 1 < Q) f[4 * j + 1] = v.y;
+                if constexpr (4 * j + 2 < Q) f[4 * j + 2] = v.z;
+                if constexpr (4 * j + 3 < Q) f[4 * j + 3] = v.w;
+            });
         }
         if constexpr (COLL == LBM_RLBM) {
             // RLBM (src/lbm/kernels/ops/collisions/collision.mojo:168-223)
@@ -494,12 +544,45 @@ __global__ void __launch_bounds__(256) step_kernel(const StepArgs a) {
 // ---------------------------------------------------------------------------------------------
 constexpr uint32_t kTileCells = 256;
 
+// Per-axis neighbour deltas of a cell of the block-per-tile layout, in cells (dc: flags, bc) and
+// in population elements (dp), with periodic wrap across the tile grid.
+template <int D>
+__device__ __forceinline__ void tile_deltas(const StepArgs& a, uint32_t bx, uint32_t by, uint32_t bz, uint32_t lx,
+                                            uint32_t ly, uint32_t lz, int32_t TQ, int32_t (&dc)[3][3],
+                                            int32_t (&dp)[3][3]) {
+    constexpr int32_t T = (int32_t)kTileCells;
+    const int32_t tx = a.lay.tx, ty = a.lay.ty, tz = a.lay.tz, txy = tx * ty;
+    const int32_t ntx = a.lay.ntx, nty = a.lay.nty, ntz = a.lay.ntz;
+    const int32_t jxm = bx > 0 ? -1 : ntx - 1, jxp = (int32_t)bx + 1 < ntx ? 1 : 1 - ntx;
+    const int32_t jym = by > 0 ? -ntx : (nty - 1) * ntx, jyp = (int32_t)by + 1 < nty ? ntx : (1 - nty) * ntx;
+    dc[0][1] = dp[0][1] = dc[1][1] = dp[1][1] = dc[2][1] = dp[2][1] = 0;
+    if (lx > 0) dc[0][0] = dp[0][0] = -1;
+    else { dc[0][0] = (tx - 1) + T * jxm; dp[0][0] = (tx - 1) + TQ * jxm; }
+    if ((int32_t)lx + 1 < tx) dc[0][2] = dp[0][2] = 1;
+    else { dc[0][2] = (1 - tx) + T * jxp; dp[0][2] = (1 - tx) + TQ * jxp; }
+    if (ly > 0) dc[1][0] = dp[1][0] = -tx;
+    else { dc[1][0] = (ty - 1) * tx + T * jym; dp[1][0] = (ty - 1) * tx + TQ * jym; }
+    if ((int32_t)ly + 1 < ty) dc[1][2] = dp[1][2] = tx;
+    else { dc[1][2] = (1 - ty) * tx + T * jyp; dp[1][2] = (1 - ty) * tx + TQ * jyp; }
+    if constexpr (D == 3) {
+        const int32_t ntxy = ntx * nty;
+        const int32_t jzm = bz > 0 ? -ntxy : (ntz - 1) * ntxy, jzp = (int32_t)bz + 1 < ntz ? ntxy : (1 - ntz) * ntxy;
+        if (lz > 0) dc[2][0] = dp[2][0] = -txy;
+        else { dc[2][0] = (tz - 1) * txy + T * jzm; dp[2][0] = (tz - 1) * txy + TQ * jzm; }
+        if ((int32_t)lz + 1 < tz) dc[2][2] = dp[2][2] = txy;
+        else { dc[2][2] = (1 - tz) * txy + T * jzp; dp[2][2] = (1 - tz) * txy + TQ * jzp; }
+    } else {
+        dc[2][0] = dc[2][2] = dp[2][0] = dp[2][2] = 0;
+    }
+}
+
 // The per-thread body of the block-per-tile step: thread `tid` of the CTA that owns tile `tile`.
-// Every lane of a warp must call it (it starts with a warp ballot); with a closure (cl, staged in
-// shared memory) every thread of the block must.
+// Every lane of a warp must call it (it starts with a warp ballot, and the learned closure `cl`,
+// staged in shared memory, is evaluated by whole warps).  Learned closure: fbuf is this warp's
+// population stash ((Q+3)/4 x 32 float4 of shared memory).
 template <class L, int METHOD, bool F16C, int COLL, int LES>
 __device__ __forceinline__ void tile_step(const StepArgs& a, const uint32_t tile, const uint32_t tid,
-                                          const ClosureDev* cl = nullptr) {
+                                          const ClosureDev* cl = nullptr, float4* fbuf = nullptr) {
     using P = Pop<F16C>;
     using S = typename P::T;
     constexpr int Q = L::Q, D = L::D, K = D + 1;
@@ -531,7 +614,7 @@ __device__ __forceinline__ void tile_step(const StepArgs& a, const uint32_t tile
     if (!clean) {
         flag = __ldg(a.flags + n);
         // is_valid_thread (src/lbm/kernels/utils/checks.mojo:55-60); the learned closure keeps
-        // every thread for its block-wide staging and warp-wide products, the invalid ones write nothing
+        // every lane for its warp-wide products, the invalid ones write nothing
         active = !((flag & 0x0F) == LBM_FLAG_SOLID || (flag & LBM_FLAG_EXCLUDE));
         if constexpr (LES != kLesLearned) {
             if (!active) return;
@@ -539,33 +622,11 @@ __device__ __forceinline__ void tile_step(const StepArgs& a, const uint32_t tile
     }
 
     // ---- per-axis neighbour deltas, in cells (flags, bc) and in population elements (f)
-    const int32_t tx = a.lay.tx, ty = a.lay.ty, tz = a.lay.tz, txy = tx * ty;
+    const int32_t tx = a.lay.tx, ty = a.lay.ty, tz = a.lay.tz;
     const uint32_t lx = tid & a.mx, ly = (tid >> a.shx) & a.my, lz = tid >> a.shxy;
     const int32_t TQ = (int32_t)(T * Q);
     int32_t dc[3][3], dp[3][3];
-    {
-        const int32_t jxm = bx > 0 ? -1 : ntx - 1, jxp = (int32_t)bx + 1 < ntx ? 1 : 1 - ntx;
-        const int32_t jym = by > 0 ? -ntx : (nty - 1) * ntx, jyp = (int32_t)by + 1 < nty ? ntx : (1 - nty) * ntx;
-        dc[0][1] = dp[0][1] = dc[1][1] = dp[1][1] = dc[2][1] = dp[2][1] = 0;
-        if (lx > 0) dc[0][0] = dp[0][0] = -1;
-        else { dc[0][0] = (tx - 1) + (int32_t)T * jxm; dp[0][0] = (tx - 1) + TQ * jxm; }
-        if ((int32_t)lx + 1 < tx) dc[0][2] = dp[0][2] = 1;
-        else { dc[0][2] = (1 - tx) + (int32_t)T * jxp; dp[0][2] = (1 - tx) + TQ * jxp; }
-        if (ly > 0) dc[1][0] = dp[1][0] = -tx;
-        else { dc[1][0] = (ty - 1) * tx + (int32_t)T * jym; dp[1][0] = (ty - 1) * tx + TQ * jym; }
-        if ((int32_t)ly + 1 < ty) dc[1][2] = dp[1][2] = tx;
-        else { dc[1][2] = (1 - ty) * tx + (int32_t)T * jyp; dp[1][2] = (1 - ty) * tx + TQ * jyp; }
-        if constexpr (D == 3) {
-            const int32_t ntxy = ntx * nty;
-            const int32_t jzm = bz > 0 ? -ntxy : (ntz - 1) * ntxy, jzp = (int32_t)bz + 1 < ntz ? ntxy : (1 - ntz) * ntxy;
-            if (lz > 0) dc[2][0] = dp[2][0] = -txy;
-            else { dc[2][0] = (tz - 1) * txy + (int32_t)T * jzm; dp[2][0] = (tz - 1) * txy + TQ * jzm; }
-            if ((int32_t)lz + 1 < tz) dc[2][2] = dp[2][2] = txy;
-            else { dc[2][2] = (1 - tz) * txy + (int32_t)T * jzp; dp[2][2] = (1 - tz) * txy + TQ * jzp; }
-        } else {
-            dc[2][0] = dc[2][2] = dp[2][0] = dp[2][2] = 0;
-        }
-    }
+    tile_deltas<D>(a, bx, by, bz, lx, ly, lz, TQ, dc, dp);
     const int32_t own = (int32_t)tid + TQ * (int32_t)tile;
     const S* fin = (const S*)a.f_in;
     S* fout = (S*)a.f_out;
@@ -629,7 +690,7 @@ __device__ __forceinline__ void tile_step(const StepArgs& a, const uint32_t tile
                               (int32_t)(by * ty + ly), (int32_t)(bz * tz + lz), a.lay, a.ddf != 0);
     }
 
-    collide<L, COLL, LES>(f, a.tau, a, a.bc + (tid + (uint64_t)T * K * tile), T, flag, active, cl);
+    collide<L, COLL, LES>(f, a.tau, a, a.bc + (tid + (uint64_t)T * K * tile), T, flag, active, cl, fbuf);
     if constexpr (LES == kLesLearned) {
         if (!active) return;
     }
@@ -654,9 +715,35 @@ __device__ __forceinline__ void tile_step(const StepArgs& a, const uint32_t tile
 }
 
 template <class L, int METHOD, bool F16C, int COLL, int LES>
-__global__ void __launch_bounds__(256, (LES == kLesLearned) ? 2 : (L::Q == 9) ? 5 : ((COLL == LBM_KBC || L::Q == 27) ? 3 : 4))
+__global__ void __launch_bounds__(256, (L::Q == 9) ? 5 : ((COLL == LBM_KBC || L::Q == 27) ? 3 : 4))
     step_kernel_tile(const StepArgs a) {
-    tile_step<L, METHOD, F16C, COLL, LES>(a, blockIdx.x, threadIdx.x, stage_closure<LES == kLesLearned>(a.closure));
+    static_assert(LES != kLesLearned, "the learned closure runs in step_kernel_learned");
+    tile_step<L, METHOD, F16C, COLL, LES>(a, blockIdx.x, threadIdx.x);
+}
+
+#ifndef LBM_LEARNED_MIN_BLOCKS
+#define LBM_LEARNED_MIN_BLOCKS 4
+#endif
+
+// The block-per-tile step with the learned closure as a persistent kernel: each CTA stages the
+// closure's fragments into shared memory once, then walks the tiles blockIdx.x, + gridDim.x, ...
+// (no block barrier inside the time step).
+// Shared-memory population stash of the learned-closure kernel: 8 warps x (Q+3)/4 x 32 float4.
+template <class L>
+struct LearnedStash {
+    static constexpr int NW = (L::Q + 3) / 4;
+    static constexpr size_t bytes = sizeof(float4) * 8 * NW * 32;  // dynamic shared memory
+};
+
+template <class L, int METHOD, bool F16C, int COLL, int LES>
+__global__ void __launch_bounds__(256, LBM_LEARNED_MIN_BLOCKS) step_kernel_learned(const StepArgs a) {
+    extern __shared__ float4 fbuf[];  // [8 warps][NW][32 lanes]
+    const ClosureDev* cl = stage_closure(a.closure);
+    __syncthreads();
+    const uint32_t ntiles = a.lay.ncells / kTileCells;
+    float4* stash = fbuf + (threadIdx.x >> 5) * LearnedStash<L>::NW * 32u;
+    for (uint32_t tile = blockIdx.x; tile < ntiles; tile += gridDim.x)
+        tile_step<L, METHOD, F16C, COLL, kLesLearned>(a, tile, threadIdx.x, cl, stash);
 }
 
 // Launcher type used by the dispatch tables.
@@ -672,6 +759,26 @@ cudaError_t launch_step(const StepArgs& a, int threads, cudaStream_t s) {
 template <class L, int METHOD, bool F16C, int COLL, int LES>
 cudaError_t launch_step_tile(const StepArgs& a, int, cudaStream_t s) {
     step_kernel_tile<L, METHOD, F16C, COLL, LES><<<a.lay.ncells / kTileCells, kTileCells, 0, s>>>(a);
+    return cudaGetLastError();
+}
+
+template <class L, int METHOD, bool F16C, int COLL, int LES>
+cudaError_t launch_step_learned(const StepArgs& a, int, cudaStream_t s) {
+    constexpr size_t smem = LearnedStash<L>::bytes;
+    auto kernel = step_kernel_learned<L, METHOD, F16C, COLL, LES>;
+    static int per_sm = 0, sms = 0;
+    if (per_sm == 0) {
+        int dev = 0;
+        cudaError_t e = cudaGetDevice(&dev);
+        if (e == cudaSuccess) e = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+        if (e == cudaSuccess) e = cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+        if (e == cudaSuccess) e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kernel, (int)kTileCells, smem);
+        if (e != cudaSuccess) return e;
+        if (per_sm < 1) per_sm = 1;
+    }
+    const uint32_t ntiles = a.lay.ncells / kTileCells;
+    const uint32_t grid = min(ntiles, (uint32_t)(sms * per_sm));
+    kernel<<<grid, kTileCells, smem, s>>>(a);
     return cudaGetLastError();
 }
 

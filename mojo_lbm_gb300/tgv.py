@@ -116,16 +116,16 @@ def features(S: torch.Tensor, rho: torch.Tensor, u: torch.Tensor, tau: float) ->
     same definitions as the collision kernel's (include/lbm_gb300.h, lbm_closure_t)."""
     S = S.double()
     s2 = sum((S[n] ** 2) * (1.0 if a == b else 2.0) for n, (a, b) in enumerate(_PAIRS))
-    snorm = torch.sqrt(2 * s2)
+    q = 2 * s2 + 1e-24
+    sq = torch.sqrt(q)
     tr = S[0] + S[3] + S[5]
     m = tr / 3
     a, b, c = S[0] - m, S[3] - m, S[5] - m
     det = a * (b * c - S[4] ** 2) - S[1] * (S[1] * c - S[4] * S[2]) + S[2] * (S[1] * S[4] - b * S[2])
     off = 2 * (S[1] ** 2 + S[2] ** 2 + S[4] ** 2)
     uu = (u.double() ** 2).sum(0)
-    x = torch.stack([torch.log(snorm + 1e-12), tr / (snorm + 1e-12), det / (snorm ** 3 + 1e-30), rho.double() - 1,
-                     torch.sqrt(uu), off / (s2 + 1e-30), torch.full_like(uu, math.log(tau - 0.5)),
-                     uu / (snorm + 1e-12)])
+    x = torch.stack([torch.log(q) / 2, tr / sq, det / (q * sq), rho.double() - 1, torch.sqrt(uu), 2 * off / q,
+                     torch.full_like(uu, math.log(tau - 0.5)), uu / sq])
     return x.reshape(8, -1).T.float().contiguous()
 
 

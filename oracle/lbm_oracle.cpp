@@ -186,7 +186,6 @@ float bf16_round(float x) {
  * S in stress order (2D xx, xy, yy; 3D xx, xy, xz, yy, yz, zz). */
 template <class R>
 void closure_features(int D, const R* S, R s2, R rho, R uu, R tau, R* x) {
-    const R snorm = std::sqrt((R)2 * s2);
     R tr, det, off;
     if (D == 3) {
         tr = S[0] + S[3] + S[5];
@@ -201,14 +200,16 @@ void closure_features(int D, const R* S, R s2, R rho, R uu, R tau, R* x) {
         det = a * b - S[1] * S[1];
         off = (R)2 * (S[1] * S[1]);
     }
-    x[0] = std::log(snorm + (R)1e-12);
-    x[1] = tr / (snorm + (R)1e-12);
-    x[2] = det / (snorm * snorm * snorm + (R)1e-30);
+    const R q = (R)2 * s2 + (R)1e-24;
+    const R sq = std::sqrt(q);
+    x[0] = std::log(q) / (R)2;
+    x[1] = tr / sq;
+    x[2] = det / (q * sq);
     x[3] = rho - (R)1;
     x[4] = std::sqrt(uu);
-    x[5] = off / (s2 + (R)1e-30);
+    x[5] = (R)2 * off / q;
     x[6] = std::log(tau - (R)0.5);
-    x[7] = uu / (snorm + (R)1e-12);
+    x[7] = uu / sq;
 }
 
 /* nu_t of the learned closure, or -1 when a normalised feature leaves the training range. */
@@ -217,7 +218,8 @@ R closure_nu(const R* x) {
     const lbm_closure_t& c = g_closure;
     float xn[8];
     for (int k = 0; k < 8; ++k) {
-        const float v = ((float)x[k] - c.feat_mean[k]) * c.feat_scale[k];
+        const float shift = -(c.feat_mean[k] * c.feat_scale[k]);
+        const float v = std::fma((float)x[k], c.feat_scale[k], shift);
         if (!(v >= c.feat_lo[k] && v <= c.feat_hi[k])) return (R)-1;
         xn[k] = bf16_round(v);
     }
