@@ -54,6 +54,15 @@ WORKLOADS = {
                                        "Re ~ U[20,200], parabolic moving-wall inlet u_max=0.05, equilibrium outlet, "
                                        "Bouzidi links on the cylinder, FP32, one persistent launch per step"),
 }
+for _les in ("learned", "smagorinsky"):
+    WORKLOADS[f"tgv256_d3q19_les_{_les}"] = dict(
+        kind="tgv", lattice="D3Q19", n=256, method="db", coll="SRT", les=True, closure=_les, f16=False,
+        Re=1600.0, U=0.05, tile=(8, 8, 4),
+        desc=f"D3Q19 SRT LES decaying Taylor-Green vortex, periodic 256^3, Re=1600, u0=0.05, FP32, "
+             + ("learned closure (MLP 8->32->32->1, BF16 tensor-core inference, FP32 accumulate; trained on "
+                "box-filtered 512^3 runs; Smagorinsky fallback outside the training range)" if _les == "learned"
+                else "Smagorinsky Cs=0.1"))
+CLOSURE_FILE = ROOT / "mojo_lbm_gb300" / "data" / "tgv_re1600_512to256_closure.npz"
 DEFAULT_WORKLOAD = "ldc3d_d3q19_256_fp32"
 
 
@@ -154,15 +163,27 @@ def build_case(wl: dict):
     n = wl["n"]
     grid = LBM_Grid(get_lattice(lat_id), n, n, n, wl["tile"])
     method = LBM_method.DOUBLE_BUFFER if wl["method"] == "db" else LBM_method.ESOTERIC_PULL
-    cfg = LBM_Config(method, collision_op=wl["coll"], LES=wl["les"], DDF_shift=wl["f16"], use_float16c=wl["f16"])
     N, D = grid.num_points, grid.D
     flags = np.zeros(N, np.uint8)
     bc = np.zeros(N * (D + 1), np.float32)
+    if wl.get("kind") == "tgv":  # periodic, all fluid; tau from Re = u0 L / nu with L = n / (2 pi)
+        cfg = LBM_Config(method, collision_op=wl["coll"], LES=True, include_moving_boundary=False)
+        return grid, cfg, flags, bc, 3.0 * wl["U"] * (n / (2 * math.pi)) / wl["Re"] + 0.5
+    cfg = LBM_Config(method, collision_op=wl["coll"], LES=wl["les"], DDF_shift=wl["f16"], use_float16c=wl["f16"])
     for s in ("-Y", "+X", "-X", "+Z", "-Z"):
         preprocess.set_exterior_walls(grid, cfg, flags, bc, s, Flags.SOLID, [0.0] * D, 1.0)
     preprocess.set_exterior_walls(grid, cfg, flags, bc, "+Y", Flags.SOLID, [wl["U"], 0.0, 0.0], 1.0)
     tau = 3.0 * wl["U"] * (n - 1) / wl["Re"] + 0.5
     return grid, cfg, flags, bc, tau
+
+
+def oracle_closure(wl: dict):
+    """The learned closure as the oracle's struct (None for other workloads)."""
+    if wl.get("closure") != "learned":
+        return None
+    import oracle
+    d = np.load(CLOSURE_FILE)
+    return oracle.closure_struct(d["theta"], float(d["nu_scale"]), d["mean"], d["scale"], d["lo"], d["hi"])
 
 
 def cpu_sample(wl: dict, grid, cfg, flags, bc, tau, budget_s: float, max_steps: int | None = None):
@@ -172,6 +193,7 @@ def cpu_sample(wl: dict, grid, cfg, flags, bc, tau, budget_s: float, max_steps: 
     N, Q = grid.num_points, grid.Q
     f = np.zeros(N * Q, oracle.f_dtype(cfg, 32))
     oracle.init(cfg, grid, 32, f)
+    oracle.set_closure(oracle_closure(wl))
     f2 = f.copy() if wl["method"] == "db" else f
     cores = oracle.max_threads()
     slab = max(1, N // 16)
@@ -183,6 +205,7 @@ def cpu_sample(wl: dict, grid, cfg, flags, bc, tau, budget_s: float, max_steps: 
         t_total += time.perf_counter() - t0
         done_cells += min(N, b + slab) - b
         k += 1
+    oracle.set_closure(None)
     return done_cells / t_total / 1e6, cores, f"{k} slab-steps of {slab} cells (1/16 of the grid) each, {t_total:.1f} s"
 
 
@@ -209,7 +232,18 @@ def run_ours(args, wl: dict):
     fb = torch.empty_like(fa) if wl["method"] == "db" else fa
     bct = torch.from_numpy(bc).to(dev)
     flt = torch.from_numpy(flags).to(dev)
-    solver.init_equilibrium(fa)
+    closure = None
+    if wl.get("kind") == "tgv":
+        from mojo_lbm_gb300 import tgv
+        from mojo_lbm_gb300.closure import LearnedClosure, set_closure
+        u0, g0 = tgv.tgv_fields(grid.nx, wl["U"], seed=0, device=dev)
+        solver.init_equilibrium(fa, 1.0, tau, u0, g0)
+        del u0, g0
+        if wl["closure"] == "learned":
+            closure = LearnedClosure.load(CLOSURE_FILE, device=dev)
+            set_closure(solver, closure)
+    else:
+        solver.init_equilibrium(fa)
     if wl["method"] == "db":
         fb.copy_(fa)
     stream = torch.cuda.current_stream(dev)
@@ -280,6 +314,31 @@ def run_ours(args, wl: dict):
     key = (wl["lattice"], wl["f16"])
     b_alg = BYTES_PER_UPDATE[key]
     achieved = b_alg * N / (launch_ms * 1e-3) / 1e9
+    extra = {}
+    if closure is not None:
+        # the Smagorinsky step on the same fields, timed the same way, for the per-step time ratio
+        from mojo_lbm_gb300 import tgv
+        smag = Solver(grid, cfg)  # the same LES configuration without the closure
+        u0, g0 = tgv.tgv_fields(grid.nx, wl["U"], seed=0, device=dev)
+        smag.init_equilibrium(fa, 1.0, tau, u0, g0)
+        del u0, g0
+        fb.copy_(fa)
+        smag.run(fa, fb, bct, flt, tau, 64, 0, stream)
+        torch.cuda.synchronize(dev)
+        s0, s1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        s0.record(stream)
+        smag.run(fa, fb, bct, flt, tau, K, 0, stream)
+        s1.record(stream)
+        torch.cuda.synchronize(dev)
+        smag_mlups = float(N) * K / (s0.elapsed_time(s1) * 1e-3) / 1e6
+        smag.close()
+        m = closure.meta
+        extra = {"smagorinsky_mlups": round(smag_mlups, 2), "time_ratio_vs_smagorinsky": round(smag_mlups / mlups, 4),
+                 "tensor_tflops": round(2624.0 * N / (launch_ms * 1e-3) / 1e12, 2),
+                 "closure_study": {k: m.get(k) for k in ("N_fine", "N_coarse", "Re", "eval_times", "spectrum_error",
+                                                         "energy_error", "time_ratio", "command")},
+                 "closure_study_note": "errors vs the box-filtered 512^3 run, recorded when the committed network "
+                                       "was trained (not re-run by this benchmark)"}
     peak, peak_kind = measured_peaks()
     traffic, traffic_src = profiled_traffic(args.workload)
     cpu = None
@@ -291,7 +350,9 @@ def run_ours(args, wl: dict):
         "metric": "D3Q19 MLUPs" if wl["lattice"] == "D3Q19" else f"{wl['lattice']} MLUPs",
         "value": round(mlups, 2), "unit": "MLUPs", "n_gpus": world, "steps": K, "warmup": args.warmup,
         "ms_per_step": round(t_ms / K, 5), "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
-        "dtype": "f16c" if wl["f16"] else "f32", "data": "synthetic (lid-driven cavity from rest)",
+        "dtype": "f16c" if wl["f16"] else "f32",
+        "data": "synthetic (Taylor-Green vortex + seeded perturbation)" if wl.get("kind") == "tgv"
+                else "synthetic (lid-driven cavity from rest)",
         "config": {"workload": wl["desc"], "grid": [grid.nx, grid.ny, grid.nz], "tile": list(grid.tile_shape),
                    "layout": "reference tiled layout (col-major tile, col-major tiler)", "tau": round(tau, 6),
                    "timing": "CUDA events around a K-step graph replay on the launching stream",
@@ -310,6 +371,7 @@ def run_ours(args, wl: dict):
         "gpu_launches": K,
         "clocks": clk,
     }
+    line.update(extra)
     print(json.dumps(line), flush=True)
     solver.close()
     if world > 1:
@@ -404,6 +466,7 @@ def run_reference(args, wl: dict):
     f = np.zeros(N * Q, oracle.f_dtype(cfg, 32))
     oracle.init(cfg, grid, 32, f)
     f2 = f.copy() if wl["method"] == "db" else f
+    # the reference's LES is Smagorinsky (it has no learned closure): its path for LES workloads
     cores = oracle.max_threads()
     slab = max(1, N // 64)
     times = []
@@ -419,9 +482,12 @@ def run_reference(args, wl: dict):
     line = {"impl": "reference", "metric": "D3Q19 MLUPs" if wl["lattice"] == "D3Q19" else f"{wl['lattice']} MLUPs",
             "value": round(v, 3), "unit": "MLUPs", "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
             "ms_per_step": round(1e3 * t / len(times), 4), "higher_is_better": True, "scaling": "weak",
-            "vs_baseline": None, "dtype": "f16c" if wl["f16"] else "f32", "data": "synthetic (lid-driven cavity)",
+            "vs_baseline": None, "dtype": "f16c" if wl["f16"] else "f32",
+            "data": "synthetic (periodic box at rest)" if wl.get("kind") == "tgv" else "synthetic (lid-driven cavity)",
             "config": {"workload": wl["desc"], "grid": [grid.nx, grid.ny, grid.nz], "tile": list(grid.tile_shape),
-                       "step_sample": f"each step updates one slab of {slab} cells (1/64 of the grid)"},
+                       "step_sample": f"each step updates one slab of {slab} cells (1/64 of the grid)",
+                       **({"reference_path": "Smagorinsky LES: the reference has no learned closure"}
+                          if wl.get("closure") == "learned" else {})},
             "cpu_baseline": {"value": round(v, 3), "unit": "MLUPs", "cores": cores, "kind": "port",
                              "sample": f"float32 CPU oracle (restatement of the reference step), {len(times)} "
                                        f"slab-steps of {slab} cells; the reference itself is Mojo and not runnable"},

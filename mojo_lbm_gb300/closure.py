@@ -134,6 +134,7 @@ class LearnedClosure:
     nu_scale: float
     norm: Normalisation
     history: list = field(default_factory=list)
+    meta: dict = field(default_factory=dict)
 
     def to_c(self) -> _capi.lbm_closure_t:
         t = self.theta.detach().float().cpu().numpy()
@@ -156,15 +157,21 @@ class LearnedClosure:
         with torch.no_grad():
             return mlp(self.theta, self.norm.apply(x_raw).contiguous(), self.nu_scale)
 
-    def save(self, path) -> None:
+    def save(self, path, meta: dict | None = None) -> None:
+        """Parameters and normalisation in an .npz; meta (a JSON-able record of how the network was
+        trained and how it scored) rides along."""
+        import json
         np.savez(path, theta=self.theta.detach().cpu().numpy(), nu_scale=self.nu_scale, mean=self.norm.mean,
-                 scale=self.norm.scale, lo=self.norm.lo, hi=self.norm.hi)
+                 scale=self.norm.scale, lo=self.norm.lo, hi=self.norm.hi, meta=json.dumps(meta or {}))
 
     @staticmethod
     def load(path, device="cuda") -> "LearnedClosure":
+        import json
         d = np.load(path)
-        return LearnedClosure(torch.tensor(d["theta"], dtype=torch.float32, device=device), float(d["nu_scale"]),
-                              Normalisation(d["mean"], d["scale"], d["lo"], d["hi"]))
+        c = LearnedClosure(torch.tensor(d["theta"], dtype=torch.float32, device=device), float(d["nu_scale"]),
+                           Normalisation(d["mean"], d["scale"], d["lo"], d["hi"]))
+        c.meta = json.loads(str(d["meta"])) if "meta" in d.files else {}
+        return c
 
 
 def train(x_raw: torch.Tensor, target: torch.Tensor, *, steps: int = 600, batch: int = 1 << 18, lr: float = 3e-3,
@@ -193,7 +200,7 @@ def train(x_raw: torch.Tensor, target: torch.Tensor, *, steps: int = 600, batch:
         opt.lr = lr * (0.05 + 0.95 * cosine(k))
         opt.step(th.grad)
         if log_every and (k % log_every == 0 or k == steps - 1):
-            closure.history.append((k, float(loss)))
+            closure.history.append((k, float(loss.detach())))
     return closure
 
 

@@ -192,7 +192,7 @@ class TGVCase:
         return 3.0 * self.u0 * self.L / self.Re + 0.5
 
     def steps(self, t_star: float) -> int:
-        return int(round(t_star * self.L / self.u0))
+        return int(round(float(t_star) * self.L / self.u0))
 
 
 class TGVRun:
@@ -347,3 +347,34 @@ def study(N_fine: int = 512, Re: float = 1600.0, u0: float = 0.05, *, train_time
         res["time_ratio"] = lt / s
     res["closure"] = closure
     return res
+
+
+def main(argv=None) -> None:
+    """Runs the comparison and prints one JSON line (and saves the trained closure with --save)."""
+    import argparse
+    import json
+    ap = argparse.ArgumentParser(description="Learned closure vs Smagorinsky on the decaying Taylor-Green vortex")
+    ap.add_argument("--fine", type=int, default=512, help="cells per side of the fine reference run")
+    ap.add_argument("--re", type=float, default=1600.0)
+    ap.add_argument("--u0", type=float, default=0.05)
+    ap.add_argument("--train-times", default="2,4,6,8,10")
+    ap.add_argument("--eval-times", default="2,4,6,8,10")
+    ap.add_argument("--train-steps", type=int, default=600)
+    ap.add_argument("--time-steps", type=int, default=400)
+    ap.add_argument("--collision", default="SRT")
+    ap.add_argument("--save", default="", help="path of an .npz for the trained closure")
+    args = ap.parse_args(argv)
+    times = lambda s: tuple(float(t) for t in s.split(","))  # noqa: E731
+    res = study(args.fine, args.re, args.u0, train_times=times(args.train_times), eval_times=times(args.eval_times),
+                train_steps=args.train_steps, time_steps=args.time_steps, collision=args.collision,
+                log=lambda *a: print(*a, flush=True))
+    closure = res.pop("closure")
+    res["train_loss"] = closure.history
+    res["command"] = "python -m mojo_lbm_gb300.tgv " + " ".join(argv if argv is not None else __import__("sys").argv[1:])
+    if args.save:
+        closure.save(args.save, meta=res)
+    print(json.dumps(res), flush=True)
+
+
+if __name__ == "__main__":
+    main()
