@@ -354,6 +354,7 @@ def run_ours(args, wl: dict):
         "data": "synthetic (Taylor-Green vortex + seeded perturbation)" if wl.get("kind") == "tgv"
                 else "synthetic (lid-driven cavity from rest)",
         "config": {"workload": wl["desc"], "grid": [grid.nx, grid.ny, grid.nz], "tile": list(grid.tile_shape),
+                   "tile_source": wl.get("tile_source", "default of the workload"),
                    "layout": "reference tiled layout (col-major tile, col-major tiler)", "tau": round(tau, 6),
                    "timing": "CUDA events around a K-step graph replay on the launching stream",
                    "l2": "no flush: the two lattices (2 x %.2f GB) exceed the 129 MB L2" % (N * Q * (2 if wl["f16"] else 4) / 1e9),
@@ -508,6 +509,8 @@ def main(argv=None):
     ap.add_argument("--n", type=int, default=0, help="cube edge override (profiling on a smaller case)")
     ap.add_argument("--cpu-seconds", type=float, default=12.0)
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--autotune", action="store_true",
+                    help="choose the layout's tile with the library's autotuner before the run")
     args = ap.parse_args(argv)
     if args.warmup < 3:
         ap.error("--warmup must be at least 3")
@@ -517,6 +520,16 @@ def main(argv=None):
     if args.n:
         wl["n"] = args.n
         wl["desc"] = wl["desc"].replace("256^3", f"{args.n}^3")
+    if args.autotune and args.impl == "ours" and not wl.get("batch"):
+        import torch
+        from mojo_lbm_gb300 import autotune
+        untiled = dict(wl, tile=(wl["n"],) * 3)
+        grid, cfg, flags, bc, _ = build_case(untiled)  # the workload's flags in the untiled layout
+        tile, _, tuned = autotune.best_tile(cfg, grid.lattice, grid.nx, grid.ny, grid.nz,
+                                            flags=torch.from_numpy(flags).cuda(), bc=torch.from_numpy(bc).cuda())
+        wl["tile"] = tile
+        wl["tile_source"] = f"autotuned ({len(autotune.candidates(grid.lattice, grid.nx, grid.ny, grid.nz))} " \
+                            f"candidate tiles timed on the workload's own flags: {tuned:.0f} MLUPs)"
     if args.impl == "reference":
         return run_reference(args, wl)
     if wl.get("batch"):

@@ -293,6 +293,31 @@ lbm_status lbm_mlp_backward(const float* theta, const float* x, const float* g, 
 lbm_status lbm_mlp_adam(float* theta, const float* grad, float* m, float* v, int32_t n_params,
                         float lr, float beta1, float beta2, float eps, int32_t t, void* stream);
 
+/* ---- autotuner ----
+ * No counterpart in the reference (its tile and block shapes are compile-time choices,
+ * grid.mojo:55-107).  lbm_tune_candidates lists the 256-cell power-of-two tiles (tx, ty, tz)
+ * that divide the grid (the layouts the block-per-tile kernel runs), writing at most max triples
+ * into tiles (may be NULL); it returns their number, or -1 for a bad lattice or shape.  No GPU is
+ * used.  lbm_autotune times every candidate tile (and both streaming methods when choose_method
+ * is non-zero) for the configuration, `steps` graph-replayed steps each from rest, and returns
+ * the fastest.  flags and bc are the caller's device arrays in the untiled layout (x fastest,
+ * then y, z, and the bc component slowest); they are laid out for each candidate.  NULL flags
+ * time a periodic box of fluid instead, which favours tiles a walled domain would not.  It
+ * allocates scratch buffers of the grid's size and frees them before returning.
+ * LBM_EUNSUPPORTED when no candidate tile divides the grid. */
+typedef struct lbm_tune_result_t {
+    int32_t tx, ty, tz;       /* fastest tile */
+    int32_t lbm_method;       /* its streaming method (the configuration's unless chosen) */
+    float mlups;              /* its measured throughput */
+    int32_t n_candidates;     /* candidates timed */
+} lbm_tune_result_t;
+
+int32_t lbm_tune_candidates(int32_t lattice, int32_t nx, int32_t ny, int32_t nz, int32_t* tiles,
+                            int32_t max);
+lbm_status lbm_autotune(const lbm_config_t* cfg, int32_t lattice, int32_t nx, int32_t ny, int32_t nz,
+                        const uint8_t* flags, const float* bc, int32_t choose_method, int32_t steps,
+                        lbm_tune_result_t* out, void* stream);
+
 /* Float16C codec (src/utils/custom_fp.mojo:36-101) over device arrays. */
 lbm_status lbm_float16c_encode(const float* in, uint16_t* out, int64_t n, void* stream);
 lbm_status lbm_float16c_decode(const uint16_t* in, float* out, int64_t n, void* stream);

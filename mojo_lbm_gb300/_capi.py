@@ -44,6 +44,11 @@ class lbm_closure_t(C.Structure):
                 ("feat_hi", C.c_float * 8)]
 
 
+class lbm_tune_result_t(C.Structure):
+    _fields_ = [("tx", C.c_int32), ("ty", C.c_int32), ("tz", C.c_int32), ("lbm_method", C.c_int32),
+                ("mlups", C.c_float), ("n_candidates", C.c_int32)]
+
+
 _vp = C.c_void_p
 _i32 = C.c_int32
 _i64 = C.c_int64
@@ -85,6 +90,9 @@ SIGNATURES = {
     "lbm_mlp_forward": (_i32, [_vp, _vp, _i64, _f32, _vp, _vp]),
     "lbm_mlp_backward": (_i32, [_vp, _vp, _vp, _i64, _f32, _vp, _vp]),
     "lbm_mlp_adam": (_i32, [_vp, _vp, _vp, _vp, _i32, _f32, _f32, _f32, _f32, _i32, _vp]),
+    "lbm_tune_candidates": (_i32, [_i32, _i32, _i32, _i32, _vp, _i32]),
+    "lbm_autotune": (_i32, [_CFG, _i32, _i32, _i32, _i32, _vp, _vp, _i32, _i32, C.POINTER(lbm_tune_result_t),
+                            _vp]),
     "lbm_float16c_encode": (_i32, [_vp, _vp, _i64, _vp]),
     "lbm_float16c_decode": (_i32, [_vp, _vp, _i64, _vp]),
     "lbm_last_error": (C.c_char_p, []),
