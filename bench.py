@@ -49,8 +49,8 @@ WORKLOADS = {
                                          desc="D3Q27 KBC + Smagorinsky Cs=0.1 lid-driven cube 256^3, Re=10000, "
                                               "Float16C + DDF shift, FP32 math, esoteric-pull in place"),
     "batch2d_cylinders_512": dict(lattice="D2Q9", n=0, method="db", coll="SRT", les=False, f16=False, batch=512,
-                                  tile=(16, 16, 1),
-                                  desc="512 D2Q9 SRT cylinder channels, nx ~ U[200,800] (16-cell tiles), ny = 0.41 nx, "
+                                  tile=(16, 16, 1), autotune=True,
+                                  desc="512 D2Q9 SRT cylinder channels, nx ~ U[200,800], ny = 0.41 nx (sizes on a 32-cell granule, tile autotuned), "
                                        "Re ~ U[20,200], parabolic moving-wall inlet u_max=0.05, equilibrium outlet, "
                                        "Bouzidi links on the cylinder, FP32, one persistent launch per step"),
 }
@@ -395,7 +395,27 @@ def run_batch(args, wl: dict):
         dist.init_process_group("nccl")
     dev = torch.device("cuda", local if world > 1 else 0)
     torch.cuda.set_device(dev)
-    chans = cylinder_channels(wl["batch"], seed=rank, tile=wl["tile"])
+    tile_source = "default of the workload"
+    if args.autotune or (wl.get("autotune") and not args.no_autotune):
+        # sizes on a 32 x 32 granule, so every candidate tile divides every channel
+        from mojo_lbm_gb300 import autotune
+        from mojo_lbm_gb300.workloads import Channel, channel_specs
+        specs = channel_specs(wl["batch"], seed=rank, granule=(32, 32))
+        by_shape = {(nx, ny): (nx, ny, Re, off) for nx, ny, Re, off in specs}
+
+        def build(shape, tile):
+            nx, ny, Re, off = by_shape[(shape[0], shape[1])]
+            ch = Channel(nx, ny, Re, 0.05, off, tuple(tile))
+            links = (ch.body.fluid_boundaries_list, ch.body.lattice_links_list, ch.body.link_distances_list)
+            return ch.grid, ch.cfg, ch.flags, ch.bc, ch.tau, links
+
+        tile, timing = autotune.batch_tile([(nx, ny, 1) for nx, ny, _, _ in specs], build)
+        wl["tile"] = tile
+        chans = cylinder_channels(tile=tile, specs=specs)
+        tile_source = ("autotuned on a batch of replicas of the median channel (" +
+                       ", ".join(f"{t[0]}x{t[1]}: {v:.0f}" for t, v in sorted(timing.items())) + " MLUPs)")
+    else:
+        chans = cylinder_channels(wl["batch"], seed=rank, tile=wl["tile"])
     cfg = chans[0].cfg
     batch = BatchSolver([c.grid for c in chans], cfg)
     keep = []
@@ -444,7 +464,8 @@ def run_batch(args, wl: dict):
         "steps": K, "warmup": args.warmup, "ms_per_step": round(t_ms / K, 5), "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded channels from rest)",
         "config": {"workload": wl["desc"], "domains": len(chans), "cells": N, "links": int(ids.numel()),
-                   "tile": list(wl["tile"]), "l2": "no flush: 2 x %.2f GB of lattices exceed L2" % (N * 36 / 1e9)},
+                   "tile": list(wl["tile"]), "tile_source": tile_source,
+                   "l2": "no flush: 2 x %.2f GB of lattices exceed L2" % (N * 36 / 1e9)},
         "roofline": {"bound": "hbm", "achieved": round(achieved, 1), "peak": peak, "unit": "GB/s",
                      "frac": round(achieved / peak, 4), "traffic": None,
                      "note": f"72 B/update x {N} cells / median per-step CUDA-event time {launch_ms:.4f} ms "
@@ -511,6 +532,7 @@ def main(argv=None):
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--autotune", action="store_true",
                     help="choose the layout's tile with the library's autotuner before the run")
+    ap.add_argument("--no-autotune", action="store_true", help="keep the workload's default tile")
     args = ap.parse_args(argv)
     if args.warmup < 3:
         ap.error("--warmup must be at least 3")

@@ -51,19 +51,25 @@ class Channel:
         self.tau = 3.0 * (2.0 / 3.0 * u_max) * self.diameter / Re + 0.5
 
 
-def cylinder_channels(n: int = 512, seed: int = 0, nx_range=(200, 800), u_max: float = 0.05, tile=(16, 16, 1)):
-    """The batch of BASELINE's fourth configuration: nx ~ U[200, 800], ny = 0.41 nx, Re ~ U[20, 200],
-    cylinder offset ~ U[-0.05, 0.05] ny; nx and ny are rounded to whole 16-cell tiles."""
+def channel_specs(n: int = 512, seed: int = 0, nx_range=(200, 800), granule=(16, 16)):
+    """(nx, ny, Re, y_offset) of the batch of BASELINE's fourth configuration: nx ~ U[200, 800],
+    ny = 0.41 nx, Re ~ U[20, 200], cylinder offset ~ U[-0.05, 0.05] ny; nx and ny rounded to
+    multiples of the granule (so that every tile dividing the granule divides every domain)."""
     rng = np.random.default_rng(seed)
     out = []
     for _ in range(n):
         nx = int(rng.integers(nx_range[0], nx_range[1] + 1))
-        nx = max(tile[0], int(round(nx / tile[0])) * tile[0])
-        ny = max(tile[1], int(round(0.41 * nx / tile[1])) * tile[1])
-        Re = float(rng.uniform(20.0, 200.0))
-        off = float(rng.uniform(-0.05, 0.05))
-        out.append(Channel(nx, ny, Re, u_max, off, tile))
+        nx = max(granule[0], int(round(nx / granule[0])) * granule[0])
+        ny = max(granule[1], int(round(0.41 * nx / granule[1])) * granule[1])
+        out.append((nx, ny, float(rng.uniform(20.0, 200.0)), float(rng.uniform(-0.05, 0.05))))
     return out
+
+
+def cylinder_channels(n: int = 512, seed: int = 0, nx_range=(200, 800), u_max: float = 0.05, tile=(16, 16, 1),
+                      granule=None, specs=None):
+    """The channels of channel_specs (granule defaults to the tile) in the given tile layout."""
+    specs = specs or channel_specs(n, seed, nx_range, granule or tile[:2])
+    return [Channel(nx, ny, Re, u_max, off, tile) for nx, ny, Re, off in specs]
 
 
 def links_of(channels, device="cuda"):

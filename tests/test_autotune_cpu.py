@@ -33,3 +33,14 @@ def test_candidates_reject_bad_shapes():
         autotune.candidates(get_D2Q9(), 64, 64, 4)
     with pytest.raises(ValueError):
         autotune.candidates(get_D3Q19(), 0, 64, 64)
+
+
+def test_channel_sizes_on_a_granule_admit_every_tile_of_the_granule():
+    from mojo_lbm_gb300.workloads import channel_specs
+    specs = channel_specs(64, seed=1, granule=(32, 32))
+    common = None
+    for nx, ny, Re, off in specs:
+        assert nx % 32 == 0 and ny % 32 == 0 and 20 <= Re <= 200 and abs(off) <= 0.05
+        c = set(autotune.candidates(get_D2Q9(), nx, ny, 1))
+        common = c if common is None else common & c
+    assert {(8, 32, 1), (16, 16, 1), (32, 8, 1)} <= common
