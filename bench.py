@@ -533,12 +533,16 @@ def main(argv=None):
     ap.add_argument("--autotune", action="store_true",
                     help="choose the layout's tile with the library's autotuner before the run")
     ap.add_argument("--no-autotune", action="store_true", help="keep the workload's default tile")
+    ap.add_argument("--domains", type=int, default=0, help="domain count override of the batched workload")
     args = ap.parse_args(argv)
     if args.warmup < 3:
         ap.error("--warmup must be at least 3")
     wl = dict(WORKLOADS[args.workload])
     if args.tile:
         wl["tile"] = tuple(int(v) for v in args.tile.split(","))
+    if args.domains and wl.get("batch"):
+        wl["batch"] = args.domains
+        wl["desc"] = wl["desc"].replace("512 D2Q9", f"{args.domains} D2Q9")
     if args.n:
         wl["n"] = args.n
         wl["desc"] = wl["desc"].replace("256^3", f"{args.n}^3")

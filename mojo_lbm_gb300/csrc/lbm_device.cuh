@@ -109,33 +109,47 @@ LBM_HD float as_f32(uint32_t u) {
 #endif
 }
 
-// Decode.  A code with a non-zero exponent field is a normal float32 whose exponent is 112 larger:
-// shifting the 15 magnitude bits up by 12 and adding 112 << 23 produces it.  A code with a zero
-// exponent field (denormal) is M * 2^-25 for its 11-bit mantissa M, exact in float32; this is
-// the value the reference's renormalisation builds bit by bit.
+// Decode.  The 15 magnitude bits shifted up by 12 are a float32 whose exponent field is the code's
+// (offset 0 instead of 112): for a normal code a float of the right mantissa and an exponent 112
+// too small, for a denormal code (zero exponent field) the float32 denormal M * 2^-137 of its
+// 11-bit mantissa M.  One multiplication by 2^112 (exact: no overflow, denormal operands are
+// kept) gives both, the latter being the M * 2^-25 that the reference's renormalisation builds
+// bit by bit.  The sign moves from bit 15 to bit 31.
 LBM_HD float f16c_decode(uint32_t h) {
-    const uint32_t mag = h & 0x7FFFu;
-    const uint32_t nrm = (mag << 12) + 0x38000000u;
-    const uint32_t den = as_u32((float)mag * 0x1p-25f);
-    return as_f32(((h & 0x8000u) << 16) | (mag >= 0x0800u ? nrm : den));
+    const uint32_t bits = ((h & 0x7FFFu) << 12) | ((h & 0x8000u) << 16);
+#if defined(__CUDA_ARCH__)
+    return __fmul_rn(as_f32(bits), 0x1p112f);
+#else
+    return as_f32(bits) * 0x1p112f;
+#endif
 }
 
-// Encode, with the reference's rounding: add 0x800 to the float32 bits (round half up on the
-// first dropped bit), then take the exponent e of the sum:
-//   e > 112       normal code ((e - 112) << 11) | (m >> 12), i.e. (|b| >> 12) - (112 << 11),
-//                 saturated to 0x7FFF when e > 127;
-//   100 < e < 113 denormal code (((0x7FF800 + m) >> (124 - e)) + 1) >> 1;
-//   e < 101       zero.
-// The sign bit is taken from the sum.  Only the low 16 bits are kept.
+// |x| * 2^-112 rounded toward zero.  For |x| >= 2^-14 the product is a normal float32 whose bits are
+// those of |x| less 112 << 23; below, it is the float32 denormal floor(|x| * 2^37) * 2^-149.
+LBM_HD uint32_t f16c_scale_down_rz(uint32_t mag_bits) {
+#if defined(__CUDA_ARCH__)
+    return as_u32(__fmul_rz(as_f32(mag_bits), 0x1p-112f));
+#else
+    const double v = (double)as_f32(mag_bits) * 0x1p-112;  // exact in double
+    if (!(v < 0x1p-126)) return as_u32((float)v);           // normal, inf or NaN: exact or any NaN
+    return (uint32_t)(v * 0x1p149);                          // denormal: truncation
+#endif
+}
+
+// Encode, with the reference's rounding (add 0x800 to the float32 bits, round half up on the first
+// dropped bit, saturate to 0x7FFF, sign from the sum).  With y = |x| * 2^-112 rounded toward zero,
+// (bits(y) + 0x800) >> 12 is the code for every magnitude: in the normal range it is
+// (|b| >> 12) - (112 << 11) with b = bits(x) + 0x800; in the denormal range it is
+// floor(|x| * 2^25 + 1/2), which is the reference's (((0x7FF800 + m) >> (124 - e)) + 1) >> 1, and 0
+// below 2^-26.  NaN and infinity saturate.  The one case apart: a NaN whose mantissa is within 0x800
+// of all ones, where adding 0x800 carries into the sign bit and the reference's code is a signed
+// zero.  (Checked against the oracle's restatement of the reference for all 2^32 inputs.)
 LBM_HD uint32_t f16c_encode(float x) {
-    const uint32_t b = as_u32(x) + 0x00000800u;
-    const uint32_t e = (b >> 23) & 0xFFu;
-    const uint32_t m = b & 0x007FFFFFu;
-    const uint32_t nrm_raw = ((b & 0x7FFFFFFFu) >> 12) - 0x38000u;
-    const uint32_t nrm = nrm_raw < 0x7FFFu ? nrm_raw : 0x7FFFu;
-    const uint32_t sh = e > 112u ? 12u : (e < 101u ? 23u : 124u - e);
-    const uint32_t den = (((0x007FF800u + m) >> sh) + 1u) >> 1;
-    const uint32_t mag = e > 112u ? nrm : (e > 100u ? den : 0u);
+    const uint32_t u = as_u32(x);
+    const uint32_t b = u + 0x00000800u;
+    uint32_t mag = (f16c_scale_down_rz(u & 0x7FFFFFFFu) + 0x00000800u) >> 12;
+    mag = mag < 0x7FFFu ? mag : 0x7FFFu;
+    mag = (b & 0x7FFFFFFFu) < 0x00000800u ? 0u : mag;
     return ((b & 0x80000000u) >> 16) | mag;
 }
 
