@@ -115,24 +115,27 @@ LBM_HD float as_f32(uint32_t u) {
 // 11-bit mantissa M.  One multiplication by 2^112 (exact: no overflow, denormal operands are
 // kept) gives both, the latter being the M * 2^-25 that the reference's renormalisation builds
 // bit by bit.  The sign moves from bit 15 to bit 31.
-LBM_HD float f16c_decode(uint32_t h) {
-    const uint32_t bits = ((h & 0x7FFFu) << 12) | ((h & 0x8000u) << 16);
+// hs is the code sign-extended to 32 bits (a signed 16-bit load gives it for free): shifted up by
+// 12 its sign copies fill bits 27..31, and the mask keeps bit 31 alone.
+LBM_HD float f16c_decode_sx(int32_t hs) {
+    const uint32_t bits = ((uint32_t)hs << 12) & 0x87FFFFFFu;
 #if defined(__CUDA_ARCH__)
     return __fmul_rn(as_f32(bits), 0x1p112f);
 #else
     return as_f32(bits) * 0x1p112f;
 #endif
 }
+LBM_HD float f16c_decode(uint32_t h) { return f16c_decode_sx((int32_t)(int16_t)(uint16_t)h); }
 
-// |x| * 2^-112 rounded toward zero.  For |x| >= 2^-14 the product is a normal float32 whose bits are
-// those of |x| less 112 << 23; below, it is the float32 denormal floor(|x| * 2^37) * 2^-149.
-LBM_HD uint32_t f16c_scale_down_rz(uint32_t mag_bits) {
+// Bits of |x| * 2^-112 rounded toward zero.  For |x| >= 2^-14 the product is a normal float32 whose
+// bits are those of |x| less 112 << 23; below, it is the float32 denormal floor(|x| * 2^37) * 2^-149.
+LBM_HD uint32_t f16c_scale_down_rz(float x) {
 #if defined(__CUDA_ARCH__)
-    return as_u32(__fmul_rz(as_f32(mag_bits), 0x1p-112f));
+    return as_u32(__fmul_rz(fabsf(x), 0x1p-112f));
 #else
-    const double v = (double)as_f32(mag_bits) * 0x1p-112;  // exact in double
-    if (!(v < 0x1p-126)) return as_u32((float)v);           // normal, inf or NaN: exact or any NaN
-    return (uint32_t)(v * 0x1p149);                          // denormal: truncation
+    const double v = (double)as_f32(as_u32(x) & 0x7FFFFFFFu) * 0x1p-112;  // exact in double
+    if (!(v < 0x1p-126)) return as_u32((float)v);  // normal, inf or NaN: exact, or a NaN (saturates)
+    return (uint32_t)(v * 0x1p149);                 // denormal: truncation
 #endif
 }
 
@@ -147,7 +150,7 @@ LBM_HD uint32_t f16c_scale_down_rz(uint32_t mag_bits) {
 LBM_HD uint32_t f16c_encode(float x) {
     const uint32_t u = as_u32(x);
     const uint32_t b = u + 0x00000800u;
-    uint32_t mag = (f16c_scale_down_rz(u & 0x7FFFFFFFu) + 0x00000800u) >> 12;
+    uint32_t mag = (f16c_scale_down_rz(x) + 0x00000800u) >> 12;
     mag = mag < 0x7FFFu ? mag : 0x7FFFu;
     mag = (b & 0x7FFFFFFFu) < 0x00000800u ? 0u : mag;
     return ((b & 0x80000000u) >> 16) | mag;

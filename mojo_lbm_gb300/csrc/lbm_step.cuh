@@ -48,8 +48,13 @@ template <> struct Pop<false> {
 };
 template <> struct Pop<true> {
     using T = uint16_t;
-    static __device__ __forceinline__ float ld(const uint16_t* p) { return f16c_decode(__ldg(p)); }
-    static __device__ __forceinline__ float ld_rw(const uint16_t* p) { return f16c_decode(*p); }
+    // signed 16-bit loads: the codes arrive sign-extended, as f16c_decode_sx wants them
+    static __device__ __forceinline__ float ld(const uint16_t* p) {
+        return f16c_decode_sx(__ldg(reinterpret_cast<const int16_t*>(p)));
+    }
+    static __device__ __forceinline__ float ld_rw(const uint16_t* p) {
+        return f16c_decode_sx(*reinterpret_cast<const int16_t*>(p));
+    }
     static __device__ __forceinline__ void st(uint16_t* p, float v) { *p = (uint16_t)f16c_encode(v); }
 };
 
