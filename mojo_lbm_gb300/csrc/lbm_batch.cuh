@@ -59,6 +59,15 @@ __global__ void __launch_bounds__(256, (L::Q == 9) ? 5 : ((COLL == LBM_KBC || L:
     }
 }
 
+// tile_near of unit u from the tile_any bytes of its domain (one thread per unit).
+__device__ __forceinline__ void batch_near_unit(const BatchArgs& b, uint32_t u, const uint8_t* tile_any,
+                                                uint8_t* tile_near) {
+    const uint32_t d = find_domain(b.unit_begin, b.ndom, u);
+    const LayoutDesc& l = b.dom[d].lay;
+    const uint32_t first = b.unit_begin[d];
+    tile_near[u] = tile_neighbourhood(tile_any + first, u - first, l.ntx, l.nty, l.ntz);
+}
+
 // tile_any of every unit of every domain; one warp per unit.
 __device__ __forceinline__ void batch_summary_unit(const BatchArgs& b, uint32_t u, uint32_t lane,
                                                    uint8_t* tile_any) {

@@ -35,6 +35,7 @@ struct lbm_batch {
     StepArgs* d_odd = nullptr;
     uint32_t* d_begin = nullptr;
     uint8_t* d_tile_any = nullptr;
+    uint8_t* d_tile_near = nullptr;
     bool dirty = true;
     BatchLaunch step = nullptr;
     // links (caller-owned device arrays, concatenated over domains)
@@ -68,6 +69,11 @@ int ilog2(int v) { int r = 0; while ((1 << r) < v) ++r; return r; }
 void drop_graphs(lbm_batch* b) {
     for (auto& kv : b->graphs) cudaGraphExecDestroy(kv.second);
     b->graphs.clear();
+}
+
+__global__ void batch_near_kernel(const BatchArgs b, const uint8_t* tile_any, uint8_t* tile_near) {
+    const uint32_t u = blockIdx.x * blockDim.x + threadIdx.x;
+    if (u < b.total_units) batch_near_unit(b, u, tile_any, tile_near);
 }
 
 __global__ void batch_summary_kernel(const BatchArgs b, uint8_t* tile_any) {
@@ -158,6 +164,7 @@ lbm_status lbm_batch_create(const lbm_config_t* cfg, int32_t n_domains, const lb
     if (e == cudaSuccess) e = cudaMalloc(&b->d_odd, sizeof(StepArgs) * n_domains);
     if (e == cudaSuccess) e = cudaMalloc(&b->d_begin, sizeof(uint32_t) * (n_domains + 1));
     if (e == cudaSuccess) e = cudaMalloc(&b->d_tile_any, units > 0 ? units : 1);
+    if (e == cudaSuccess) e = cudaMalloc(&b->d_tile_near, units > 0 ? units : 1);
     if (e == cudaSuccess)
         e = cudaMemcpy(b->d_begin, begin.data(), sizeof(uint32_t) * (n_domains + 1), cudaMemcpyHostToDevice);
     if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&b->capture_stream, cudaStreamNonBlocking);
@@ -176,6 +183,7 @@ lbm_status lbm_batch_destroy(lbm_batch* b) {
     cudaFree(b->d_odd);
     cudaFree(b->d_begin);
     cudaFree(b->d_tile_any);
+    cudaFree(b->d_tile_near);
     if (b->capture_stream) cudaStreamDestroy(b->capture_stream);
     delete b;
     return LBM_OK;
@@ -213,7 +221,7 @@ lbm_status lbm_batch_set_domain(lbm_batch* b, int32_t i, void* f_a, void* f_b, f
     a.eqbc = b->cfg.include_equilibrium_bc;
     a.cap_rho = b->cfg.capture_density;
     a.cap_u = b->cfg.capture_velocity;
-    a.tile_any = b->d_tile_any + b->unit_begin[i];
+    a.tile_near = b->d_tile_near + b->unit_begin[i];
     a.mx = (uint32_t)g.tx - 1u;
     a.my = (uint32_t)g.ty - 1u;
     a.shx = (uint32_t)ilog2(g.tx);
@@ -276,6 +284,8 @@ lbm_status lbm_batch_run(lbm_batch* b, int64_t n_steps, int64_t first_step, void
         a.total_units = b->unit_begin.back();
         const uint32_t blocks = (uint32_t)(((uint64_t)a.total_units * 32 + 255) / 256);
         if (blocks) batch_summary_kernel<<<blocks, 256, 0, s>>>(a, b->d_tile_any);
+        LBM_BCK(cudaGetLastError());
+        if (blocks) batch_near_kernel<<<(a.total_units + 255u) / 256u, 256, 0, s>>>(a, b->d_tile_any, b->d_tile_near);
         LBM_BCK(cudaGetLastError());
     }
     const int64_t chunk = 64;

@@ -41,6 +41,14 @@ __global__ void __launch_bounds__(256) tile_summary_kernel(const uint8_t* __rest
     if (lane == 0) tile_any[warp] = any != 0u;
 }
 
+// tile_near[t]: the neighbourhood of tile t holds a non-FLUID flag; one thread per tile.
+__global__ void __launch_bounds__(256) tile_near_kernel(const uint8_t* __restrict__ tile_any, uint32_t ntiles,
+                                                        int32_t ntx, int32_t nty, int32_t ntz,
+                                                        uint8_t* __restrict__ tile_near) {
+    const uint32_t t = blockIdx.x * blockDim.x + threadIdx.x;
+    if (t < ntiles) tile_near[t] = tile_neighbourhood(tile_any, t, ntx, nty, ntz);
+}
+
 
 thread_local std::string g_err;
 
@@ -78,6 +86,7 @@ struct lbm_handle {
     StepLaunch step_learned;  // block-per-tile kernel with the learned closure (LES handles), or null
     int path;              // 0 auto, 1 generic only, 2 block-per-tile only
     uint8_t* tile_any;     // per-tile "has a non-FLUID flag" bytes for the block-per-tile kernel
+    uint8_t* tile_near;    // the same over each tile's 3x3x3 neighbourhood
     uint32_t ntiles;
     uint32_t mx, my, shx, shxy;
     int threads;
@@ -127,7 +136,7 @@ StepArgs step_args(const lbm_handle* h, const void* f_in, void* f_out, float* bc
     a.even = even;
     a.closure = h->closure_on ? h->closure : nullptr;
     a.cl = h->closure_uniform;
-    a.tile_any = h->tile_any;
+    a.tile_near = h->tile_near;
     a.mx = h->mx;
     a.my = h->my;
     a.shx = h->shx;
@@ -147,6 +156,9 @@ StepLaunch step_fn(const lbm_handle* h) {
 lbm_status tile_summary(lbm_handle* h, const uint8_t* flags, cudaStream_t s) {
     const uint32_t blocks = (h->ntiles * 32u + 255u) / 256u;
     tile_summary_kernel<<<blocks, 256, 0, s>>>(flags, h->ntiles, h->lay.T, h->tile_any);
+    LBM_CK(cudaGetLastError());
+    tile_near_kernel<<<(h->ntiles + 255u) / 256u, 256, 0, s>>>(h->tile_any, h->ntiles, h->lay.ntx, h->lay.nty,
+                                                                h->lay.ntz, h->tile_near);
     LBM_CK(cudaGetLastError());
     return LBM_OK;
 }
@@ -276,6 +288,7 @@ lbm_status lbm_create(const lbm_config_t* cfg, const lbm_grid_t* grid, lbm_handl
     h->shx = (uint32_t)ilog2(grid->tx);
     h->shxy = (uint32_t)(ilog2(grid->tx) + ilog2(grid->ty));
     h->tile_any = nullptr;
+    h->tile_near = nullptr;
     h->threads = 256;
     h->scratch = nullptr;
     h->closure = nullptr;
@@ -287,6 +300,7 @@ lbm_status lbm_create(const lbm_config_t* cfg, const lbm_grid_t* grid, lbm_handl
     if (e == cudaSuccess) e = cudaMalloc(&h->scratch, sizeof(double) * (kReduceBlocks * kReduceWidth + 8));
     if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&h->capture_stream, cudaStreamNonBlocking);
     if (e == cudaSuccess && h->step_tile) e = cudaMalloc(&h->tile_any, h->ntiles);
+    if (e == cudaSuccess && h->step_tile) e = cudaMalloc(&h->tile_near, h->ntiles);
     if (e != cudaSuccess) {
         lbm_destroy(h);
         return fail(LBM_ECUDA, std::string("lbm_create: ") + cudaGetErrorString(e));
@@ -300,6 +314,7 @@ lbm_status lbm_destroy(lbm_handle* h) {
     for (auto& kv : h->graphs) cudaGraphExecDestroy(kv.second);
     if (h->scratch) cudaFree(h->scratch);
     if (h->tile_any) cudaFree(h->tile_any);
+    if (h->tile_near) cudaFree(h->tile_near);
     if (h->closure) cudaFree(h->closure);
     if (h->capture_stream) cudaStreamDestroy(h->capture_stream);
     delete h;

@@ -181,47 +181,65 @@ __device__ __forceinline__ float warp_closure_nu(const ClosureDev* __restrict__ 
     __syncwarp();
     const uint32_t* st = reinterpret_cast<const uint32_t*>(stage);
 #if LBM_CLOSURE_INTERLEAVE
-    // layer 1: rows = cells 16 mt + g (+8), columns = features 2t, 2t+1 (K padded to 16)
-    uint32_t a[2][2][4];  // [mt][k-slice]
+    // Layer by layer, each layer's n-tiles in pairs: a pair (2kc, 2kc+1) of one layer's output is
+    // k-slice kc of the next layer's input, so it is packed (ReLU, BF16) and consumed before the
+    // next pair is computed.  16 accumulators live at a time instead of 32; the products and their
+    // accumulation order are those of a layer-at-a-time evaluation.
+    uint32_t a1[2][4];  // [mt]: layer-1 A fragments, rows = cells 16 mt + g (+8), K padded to 16
 #pragma unroll
     for (int mt = 0; mt < 2; ++mt) {
-        a[mt][0][0] = st[(16 * mt + g) * 4 + t];
-        a[mt][0][1] = st[(16 * mt + g + 8) * 4 + t];
-        a[mt][0][2] = a[mt][0][3] = 0u;
+        a1[mt][0] = st[(16 * mt + g) * 4 + t];
+        a1[mt][1] = st[(16 * mt + g + 8) * 4 + t];
+        a1[mt][2] = a1[mt][3] = 0u;
     }
-    float h[2][4][4];  // [mt][n-tile][accumulator]
+    uint32_t a2[2][2][4];  // [mt][k-slice]: layer-2 A fragments
 #pragma unroll
-    for (int nt = 0; nt < 4; ++nt) {
-        const float4 bb = c->b1q[nt][lane];
-        const uint2 w = c->w1f[nt][lane];
+    for (int kc = 0; kc < 2; ++kc) {
+        float h[2][2][4];  // [mt][j][accumulator] of layer-1 n-tile 2kc + j
 #pragma unroll
-        for (int mt = 0; mt < 2; ++mt) mma_bf16_16816_bias(h[mt][nt], a[mt][0], w, bb);
-    }
+        for (int j = 0; j < 2; ++j) {
+            const float4 bb = c->b1q[2 * kc + j][lane];
+            const uint2 w = c->w1f[2 * kc + j][lane];
 #pragma unroll
-    for (int mt = 0; mt < 2; ++mt) relu_to_a(h[mt], a[mt]);
-#pragma unroll
-    for (int nt = 0; nt < 4; ++nt) {  // layer 2
-        const float4 bb = c->b2q[nt][lane];
-        const uint4 ww = c->w2f[nt][lane];
-        const uint2 w0 = make_uint2(ww.x, ww.y), w1 = make_uint2(ww.z, ww.w);
+            for (int mt = 0; mt < 2; ++mt) mma_bf16_16816_bias(h[mt][j], a1[mt], w, bb);
+        }
 #pragma unroll
         for (int mt = 0; mt < 2; ++mt) {
-            mma_bf16_16816_bias(h[mt][nt], a[mt][0], w0, bb);
-            mma_bf16_16816(h[mt][nt], a[mt][1], w1);
+            a2[mt][kc][0] = relu_bf16x2(h[mt][0][0], h[mt][0][1]);
+            a2[mt][kc][1] = relu_bf16x2(h[mt][0][2], h[mt][0][3]);
+            a2[mt][kc][2] = relu_bf16x2(h[mt][1][0], h[mt][1][1]);
+            a2[mt][kc][3] = relu_bf16x2(h[mt][1][2], h[mt][1][3]);
+        }
+    }
+    const uint4 w3 = c->w3f[lane];  // layer 3 (output column 0), k-slice 0 in .x .y, 1 in .z .w
+    float y[2][4];
+#pragma unroll
+    for (int kc = 0; kc < 2; ++kc) {
+        float h[2][2][4];  // [mt][j][accumulator] of layer-2 n-tile 2kc + j
+#pragma unroll
+        for (int j = 0; j < 2; ++j) {
+            const float4 bb = c->b2q[2 * kc + j][lane];
+            const uint4 ww = c->w2f[2 * kc + j][lane];
+#pragma unroll
+            for (int mt = 0; mt < 2; ++mt) {
+                mma_bf16_16816_bias(h[mt][j], a2[mt][0], make_uint2(ww.x, ww.y), bb);
+                mma_bf16_16816(h[mt][j], a2[mt][1], make_uint2(ww.z, ww.w));
+            }
+        }
+        const uint2 w3k = kc == 0 ? make_uint2(w3.x, w3.y) : make_uint2(w3.z, w3.w);
+#pragma unroll
+        for (int mt = 0; mt < 2; ++mt) {
+            const uint32_t a3[4] = {relu_bf16x2(h[mt][0][0], h[mt][0][1]), relu_bf16x2(h[mt][0][2], h[mt][0][3]),
+                                    relu_bf16x2(h[mt][1][0], h[mt][1][1]), relu_bf16x2(h[mt][1][2], h[mt][1][3])};
+            if (kc == 0) mma_bf16_16816_bias(y[mt], a3, w3k, c->b3q);
+            else mma_bf16_16816(y[mt], a3, w3k);
         }
     }
 #pragma unroll
-    for (int mt = 0; mt < 2; ++mt) relu_to_a(h[mt], a[mt]);
-    const uint4 w3 = c->w3f[lane];  // layer 3 (output column 0)
-    const uint2 w30 = make_uint2(w3.x, w3.y), w31 = make_uint2(w3.z, w3.w);
-#pragma unroll
     for (int mt = 0; mt < 2; ++mt) {
-        float y[4];
-        mma_bf16_16816_bias(y, a[mt][0], w30, c->b3q);
-        mma_bf16_16816(y, a[mt][1], w31);
         if (t == 0u) {  // rows g and g + 8 of this tile
-            ys[16 * mt + g] = y[0];
-            ys[16 * mt + g + 8] = y[2];
+            ys[16 * mt + g] = y[mt][0];
+            ys[16 * mt + g + 8] = y[mt][2];
         }
     }
 #else

@@ -33,7 +33,8 @@ struct StepArgs {
     // block-per-tile path (256-cell tiles with power-of-two sides)
     const ClosureDev* closure; // learned LES closure's fragments (learned-closure kernels only)
     ClosureUniform cl;         // and its warp-uniform part
-    const uint8_t* tile_any;   // per tile: 1 if any flag of the tile is not FLUID (0)
+    const uint8_t* tile_near;  // per tile: 1 if a flag of the tile or of one of its 26 neighbours
+                               // (periodic) is not FLUID
     uint32_t mx, my, shx, shxy; // lx = t & mx, ly = (t >> shx) & my, lz = t >> shxy
 };
 
@@ -111,7 +112,7 @@ __device__ __forceinline__ void feq_visit(float rho, const float* u, float uu, F
     constexpr int Q = L::Q;
     const float c15 = 1.5f * uu;
     auto emit = [&](auto qc, float wr, float wm, float t3, float t45) {
-        const float plain = (!DDF || BOTH) ? wr * (((1.f + t3) + t45) - c15) : 0.f;
+        [[maybe_unused]] const float plain = (!DDF || BOTH) ? wr * (((1.f + t3) + t45) - c15) : 0.f;
         if constexpr (DDF) {
             const float shifted = wr * ((t3 + t45) - c15) + wm;
             if constexpr (BOTH) fn(qc, shifted, plain);
@@ -581,13 +582,30 @@ __device__ __forceinline__ void tile_deltas(const StepArgs& a, uint32_t bx, uint
     }
 }
 
+// 1 if tile t (tile grid ntx x nty x ntz, periodic) or one of its 26 neighbours holds a non-FLUID
+// flag, from the per-tile bytes `any`: the block-per-tile step skips every flag load when 0.
+__device__ __forceinline__ uint8_t tile_neighbourhood(const uint8_t* __restrict__ any, uint32_t t, int32_t ntx,
+                                                      int32_t nty, int32_t ntz) {
+    const int32_t bx = (int32_t)(t % (uint32_t)ntx), byz = (int32_t)(t / (uint32_t)ntx);
+    const int32_t by = byz % nty, bz = byz / nty;
+    uint32_t r = 0u;
+    for (int32_t oz = -1; oz <= 1; ++oz)
+        for (int32_t oy = -1; oy <= 1; ++oy)
+            for (int32_t ox = -1; ox <= 1; ++ox) {
+                const int32_t x = (bx + ox + ntx) % ntx, y = (by + oy + nty) % nty, z = (bz + oz + ntz) % ntz;
+                r |= __ldg(any + (x + ntx * (y + nty * z)));
+            }
+    return r != 0u;
+}
+
 // The per-thread body of the block-per-tile step: thread `tid` of the CTA that owns tile `tile`.
-// Every lane of a warp must call it (it starts with a warp ballot, and the learned closure `cl`,
-// staged in shared memory, is evaluated by whole warps).  Learned closure: fbuf is this warp's
+// Every lane of a warp must call it (the learned closure `cl`, staged in shared memory, is
+// evaluated by whole warps).  Learned closure: fbuf is this warp's
 // population stash ((Q+3)/4 x 32 float4 of shared memory).
 template <class L, int METHOD, bool F16C, int COLL, int LES>
 __device__ __forceinline__ void tile_step(const StepArgs& a, const uint32_t tile, const uint32_t tid,
-                                          const ClosureDev* cl = nullptr, float4* fbuf = nullptr) {
+                                          const ClosureDev* cl = nullptr, float4* fbuf = nullptr,
+                                          int32_t near = -1) {
     using P = Pop<F16C>;
     using S = typename P::T;
     constexpr int Q = L::Q, D = L::D, K = D + 1;
@@ -599,20 +617,11 @@ __device__ __forceinline__ void tile_step(const StepArgs& a, const uint32_t tile
     const uint32_t bx = tile - byz * (uint32_t)a.lay.ntx;
     const uint32_t bz = a.lay.d_nty.div(byz);
     const uint32_t by = byz - bz * (uint32_t)a.lay.nty;
-    const int32_t ntx = a.lay.ntx, nty = a.lay.nty, ntz = a.lay.ntz;
 
-    // ---- is this warp's neighbourhood all FLUID?  (lanes 0..26: the 3x3x3 tile block)
-    const uint32_t lane = tid & 31u;
-    uint32_t special = 0u;
-    if (lane < 27u) {
-        const int32_t ox = (int32_t)(lane % 3u) - 1, oy = (int32_t)((lane / 3u) % 3u) - 1, oz = (int32_t)(lane / 9u) - 1;
-        int32_t tx_ = (int32_t)bx + ox, ty_ = (int32_t)by + oy, tz_ = (int32_t)bz + oz;
-        tx_ = tx_ < 0 ? tx_ + ntx : (tx_ >= ntx ? tx_ - ntx : tx_);
-        ty_ = ty_ < 0 ? ty_ + nty : (ty_ >= nty ? ty_ - nty : ty_);
-        tz_ = tz_ < 0 ? tz_ + ntz : (tz_ >= ntz ? tz_ - ntz : tz_);
-        special = __ldg(a.tile_any + (tx_ + ntx * (ty_ + nty * tz_)));
-    }
-    const bool clean = __ballot_sync(0xffffffffu, special != 0u) == 0u;
+    // ---- is the tile's neighbourhood all FLUID?  (one byte per tile, block-uniform)
+    // (the vote makes the value warp-uniform to the compiler: uniform branches below)
+    const bool clean =
+        __all_sync(0xffffffffu, (near >= 0 ? (uint32_t)near : (uint32_t)__ldg(a.tile_near + tile)) == 0u);
 
     uint8_t flag = 0;
     bool active = true;
@@ -747,8 +756,14 @@ __global__ void __launch_bounds__(256, LBM_LEARNED_MIN_BLOCKS) step_kernel_learn
     __syncthreads();
     const uint32_t ntiles = a.lay.ncells / kTileCells;
     float4* stash = fbuf + (threadIdx.x >> 5) * LearnedStash<L>::NW * 32u;
-    for (uint32_t tile = blockIdx.x; tile < ntiles; tile += gridDim.x)
-        tile_step<L, METHOD, F16C, COLL, kLesLearned>(a, tile, threadIdx.x, cl, stash);
+    // the next tile's neighbourhood byte is loaded one tile ahead
+    int32_t near_next = blockIdx.x < ntiles ? __ldg(a.tile_near + blockIdx.x) : 0;
+    for (uint32_t tile = blockIdx.x; tile < ntiles; tile += gridDim.x) {
+        const int32_t near = near_next;
+        const uint32_t next = tile + gridDim.x;
+        near_next = next < ntiles ? __ldg(a.tile_near + next) : 0;
+        tile_step<L, METHOD, F16C, COLL, kLesLearned>(a, tile, threadIdx.x, cl, stash, near);
+    }
 }
 
 // Launcher type used by the dispatch tables.
