@@ -177,6 +177,16 @@ lbm_status lbm_init_equilibrium(lbm_handle* h, void* f, float rho, float tau, co
 lbm_status lbm_compute_rho_u(lbm_handle* h, float* rho, float* u, const void* f, const float* bc,
                              const uint8_t* flags, int32_t after_odd_step, void* stream);
 
+/* calculate_Q_criterion (output/Q_criterion.mojo:90-216): Q = |omega|^2 / 4 - |S|^2 / 2 into
+ * q ([nx][ny][nz] floats, row-major), at every cell whose flag is not SOLID (raw compare; other
+ * cells are left untouched).  S is the strain rate from the non-equilibrium second moment of the
+ * next step's streamed populations (with boundary conditions) and `tau`; omega the curl of u
+ * ([D][nx][ny][nz], as lbm_compute_rho_u writes it) by the reference's finite differences:
+ * one-sided over 1 cell, or 1/2 toward a SOLID neighbour, weighted by the other side's spacing,
+ * which makes a derivative across a non-periodic domain edge 0. */
+lbm_status lbm_q_criterion(lbm_handle* h, float* q, const void* f, const float* bc, const uint8_t* flags,
+                           const float* u, float tau, int32_t after_odd_step, void* stream);
+
 /* Mass and momentum of all non-solid, non-excluded cells, reduced in float64 on the device:
  * out = {sum rho, sum rho*u_x, sum rho*u_y, sum rho*u_z}.  Synchronises the stream.
  * Returns LBM_ENAN if any reduced value is not finite. */

@@ -75,6 +75,7 @@ SIGNATURES = {
     "lbm_run": (_i32, [_vp, _vp, _vp, _vp, _vp, _f32, _i64, _i64, _vp]),
     "lbm_init_equilibrium": (_i32, [_vp, _vp, _f32, _f32, _vp, _vp, _vp]),
     "lbm_compute_rho_u": (_i32, [_vp, _vp, _vp, _vp, _vp, _vp, _i32, _vp]),
+    "lbm_q_criterion": (_i32, [_vp, _vp, _vp, _vp, _vp, _vp, _f32, _i32, _vp]),
     "lbm_reduce_mass_momentum": (_i32, [_vp, _vp, _vp, _i32, C.POINTER(C.c_double), _vp]),
     "lbm_reduce_mass_momentum_noalloc": (_i32, [_CFG, _GRID, _vp, _vp, _i32, C.POINTER(C.c_double), _vp]),
     "lbm_linkwise_bounceback": (_i32, [_vp, _vp, _vp, _vp, _vp, _vp, _i64, _i32, _i32, _f32, _vp]),

@@ -165,13 +165,63 @@ struct RhoUArgs {
     const float* bc;
     const uint8_t* flags;
     float* rho;
-    float* u;
+    float* u;        // [D][nx][ny][nz]: written by the rho/u pass, read by the Q-criterion pass
+    float* q;        // [nx][ny][nz]: Q-criterion output
+    float tau;       // Q-criterion: the tau of the strain-rate reconstruction
     int32_t ddf, moving, eqbc, even;
 };
 
+// get_velocity_gradient (src/lbm/kernels/utils/finite_difference.mojo:14-90), dx = 1: component
+// `comp` of the stored velocity differentiated along `axis` at (x, y, z).  Each neighbour inside
+// the grid gives a one-sided difference over a spacing of 1, or 1/2 when it is SOLID (raw flag
+// compare), weighted (1 - own spacing / sum of spacings).  A neighbour outside the grid gives
+// spacing 0, which gives the other side weight 0: the reference's weighting, kept as it is,
+// returns 0 across a non-periodic domain edge.
+template <int D>
+__device__ __forceinline__ float velocity_gradient(const RhoUArgs& a, int32_t x, int32_t y, int32_t z, int comp,
+                                                   int axis) {
+    const LayoutDesc& l = a.lay;
+    const uint32_t N = l.ncells;
+    auto u_at = [&](int32_t i, int32_t j, int32_t k) {
+        return a.u[(size_t)N * comp + ((uint32_t)i * (uint32_t)l.ny + (uint32_t)j) * (uint32_t)l.nz + (uint32_t)k];
+    };
+    auto flag_at = [&](int32_t i, int32_t j, int32_t k) {
+        const uint32_t tile = (uint32_t)(i / l.tx) + (uint32_t)l.ntx * ((uint32_t)(j / l.ty) + (uint32_t)l.nty * (uint32_t)(k / l.tz));
+        const uint32_t loc = (uint32_t)(i % l.tx) + (uint32_t)l.tx * ((uint32_t)(j % l.ty) + (uint32_t)l.ty * (uint32_t)(k % l.tz));
+        return a.flags[loc + l.T * tile];
+    };
+    const int32_t g[3] = {x, y, z}, ng[3] = {l.nx, l.ny, l.nz};
+    const float u2 = u_at(x, y, z);
+    float lgrad = 0.f, ldx = 0.f, rgrad = 0.f, rdx = 0.f;
+    int32_t p[3] = {g[0], g[1], g[2]};
+    p[axis] = g[axis] - 1;
+    const bool vl = p[axis] >= 0;
+    if (vl) {
+        const float gdx = flag_at(p[0], p[1], p[2]) == LBM_FLAG_SOLID ? 0.5f : 1.f;
+        lgrad = (u2 - u_at(p[0], p[1], p[2])) * (1.f / gdx);
+        ldx = gdx;
+    }
+    p[axis] = g[axis] + 1;
+    const bool vr = p[axis] < ng[axis];
+    if (vr) {
+        const float gdx = flag_at(p[0], p[1], p[2]) == LBM_FLAG_SOLID ? 0.5f : 1.f;
+        rgrad = (u_at(p[0], p[1], p[2]) - u2) * (1.f / gdx);
+        rdx = gdx;
+    }
+    if (!vl && !vr) return 0.f;
+    const float total = ldx + rdx;
+    const float lw = 1.f - ldx / total;
+    const float rw = 1.f - lw;
+    return rgrad * rw + lgrad * lw;
+}
+
 // calculate_rho_and_velocity (src/lbm/output/velocity.mojo:25-125): the next step's stream and
 // boundary conditions, then density and velocity; SOLID cells (raw compare) report their bc.
-template <class L, bool F16C, bool ESO>
+// With QCRIT, calculate_Q_criterion (src/lbm/output/Q_criterion.mojo:90-216) instead: the same
+// stream and boundary conditions, the strain rate from the non-equilibrium second moment (tau of
+// the call), the vorticity from finite differences of the stored velocity a.u, and
+// Q = |omega|^2 / 4 - |S|^2 / 2 at every cell whose raw flag is not SOLID (others untouched).
+template <class L, bool F16C, bool ESO, bool QCRIT = false>
 __global__ void rho_u_kernel(const RhoUArgs a) {
     using P = Pop<F16C>;
     using S = typename P::T;
@@ -184,8 +234,10 @@ __global__ void rho_u_kernel(const RhoUArgs a) {
     const uint8_t flag = a.flags[n];
     const uint64_t own_bc = c.loc + (uint64_t)T * K * c.tile;
     if (flag == LBM_FLAG_SOLID) {
-        static_for<0, D>([&](auto dc) { a.u[(size_t)N * dc.value + c.r] = a.bc[own_bc + (uint64_t)T * dc.value]; });
-        a.rho[c.r] = a.bc[own_bc + (uint64_t)T * D];
+        if constexpr (!QCRIT) {
+            static_for<0, D>([&](auto dc) { a.u[(size_t)N * dc.value + c.r] = a.bc[own_bc + (uint64_t)T * dc.value]; });
+            a.rho[c.r] = a.bc[own_bc + (uint64_t)T * D];
+        }
         return;
     }
     const S* fin = (const S*)a.f;
@@ -273,8 +325,51 @@ __global__ void rho_u_kernel(const RhoUArgs a) {
             else if constexpr (L::c(q, d) < 0) mom[d] -= f[q];
         });
     });
-    a.rho[c.r] = rho;
-    static_for<0, D>([&](auto dc) { a.u[(size_t)N * dc.value + c.r] = mom[dc.value] / rho; });
+    if constexpr (!QCRIT) {
+        a.rho[c.r] = rho;
+        static_for<0, D>([&](auto dc) { a.u[(size_t)N * dc.value + c.r] = mom[dc.value] / rho; });
+    } else {
+        // get_f_noneq_vec (post_collision False), get_non_eq_second_order_moment,
+        // get_strain_rate_tensor and its norm (kernels/utils/{equilibrium,moment}.mojo), as collide
+        float u[3] = {0.f, 0.f, 0.f};
+        static_for<0, D>([&](auto dc) { u[dc.value] = mom[dc.value] / rho; });
+        float uu = 0.f;
+        static_for<0, D>([&](auto dc) { uu += u[dc.value] * u[dc.value]; });
+        float P[L::NS];
+        static_for<0, L::NS>([&](auto nc) { P[nc.value] = 0.f; });
+        for_each_feq<L>(rho, u, uu, ddf, [&](auto qc, float e) {
+            constexpr int q = decltype(qc)::value;
+            const float fn = f[q] - e;
+            static_for<0, L::NS>([&](auto nc) {
+                constexpr int n = nc.value;
+                constexpr int cc = L::c(q, sa<L>(n)) * L::c(q, sb<L>(n));
+                if constexpr (cc > 0) P[n] += fn;
+                else if constexpr (cc < 0) P[n] -= fn;
+            });
+        });
+        const float k = -1.f / (2.f * rho * (float)(1.0 / 3.0) * a.tau);
+        float s2 = 0.f;
+        static_for<0, L::NS>([&](auto nc) {
+            constexpr int n = nc.value;
+            const float Sn = P[n] * k;
+            if constexpr (sa<L>(n) != sb<L>(n)) s2 += (Sn * Sn) * 2.f;
+            else s2 += Sn * Sn;
+        });
+        // calculate_vorticity (Q_criterion.mojo:26-85) and Vector.norm_squared (sequential sum)
+        float w2 = 0.f;
+        if constexpr (D == 2) {
+            const float wz = velocity_gradient<D>(a, c.x, c.y, c.z, 1, 0) - velocity_gradient<D>(a, c.x, c.y, c.z, 0, 1);
+            w2 += wz * wz;
+        } else {
+            const float wx = velocity_gradient<D>(a, c.x, c.y, c.z, 2, 1) - velocity_gradient<D>(a, c.x, c.y, c.z, 1, 2);
+            const float wy = velocity_gradient<D>(a, c.x, c.y, c.z, 0, 2) - velocity_gradient<D>(a, c.x, c.y, c.z, 2, 0);
+            const float wz = velocity_gradient<D>(a, c.x, c.y, c.z, 1, 0) - velocity_gradient<D>(a, c.x, c.y, c.z, 0, 1);
+            w2 += wx * wx;
+            w2 += wy * wy;
+            w2 += wz * wz;
+        }
+        a.q[c.r] = 0.25f * w2 - 0.5f * s2;
+    }
 }
 
 // ---- float64 reductions ---------------------------------------------------------------------

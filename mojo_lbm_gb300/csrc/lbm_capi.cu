@@ -483,6 +483,40 @@ lbm_status lbm_init_equilibrium(lbm_handle* h, void* f, float rho, float tau, co
     });
 }
 
+lbm_status lbm_q_criterion(lbm_handle* h, float* q, const void* f, const float* bc, const uint8_t* flags,
+                           const float* u, float tau, int32_t after_odd_step, void* stream) {
+    if (check_handle(h)) return LBM_EINVAL;
+    if (!q || !u || !f || !bc || !flags) return fail(LBM_EINVAL, "null buffer");
+    RhoUArgs a;
+    a.lay = h->lay;
+    a.f = f;
+    a.bc = bc;
+    a.flags = flags;
+    a.rho = nullptr;
+    a.u = const_cast<float*>(u);  // read only in this pass
+    a.q = q;
+    a.tau = tau;
+    a.ddf = h->cfg.DDF_shift;
+    a.moving = h->cfg.include_moving_boundary;
+    a.eqbc = h->cfg.include_equilibrium_bc;
+    a.even = after_odd_step ? 1 : 0;
+    const bool f16 = h->cfg.use_float16c != 0, eso = h->cfg.lbm_method == LBM_ESOTERIC_PULL;
+    cudaStream_t s = (cudaStream_t)stream;
+    const uint32_t nb = blocks_for(h->lay.ncells, 256);
+    return dispatch_lattice(h->grid.lattice, [&](auto Lt) -> lbm_status {
+        using L = decltype(Lt);
+        if (f16) {
+            if (eso) rho_u_kernel<L, true, true, true><<<nb, 256, 0, s>>>(a);
+            else rho_u_kernel<L, true, false, true><<<nb, 256, 0, s>>>(a);
+        } else {
+            if (eso) rho_u_kernel<L, false, true, true><<<nb, 256, 0, s>>>(a);
+            else rho_u_kernel<L, false, false, true><<<nb, 256, 0, s>>>(a);
+        }
+        LBM_CK(cudaGetLastError());
+        return LBM_OK;
+    });
+}
+
 lbm_status lbm_compute_rho_u(lbm_handle* h, float* rho, float* u, const void* f, const float* bc,
                              const uint8_t* flags, int32_t after_odd_step, void* stream) {
     if (check_handle(h)) return LBM_EINVAL;
@@ -494,6 +528,8 @@ lbm_status lbm_compute_rho_u(lbm_handle* h, float* rho, float* u, const void* f,
     a.flags = flags;
     a.rho = rho;
     a.u = u;
+    a.q = nullptr;
+    a.tau = 0.f;
     a.ddf = h->cfg.DDF_shift;
     a.moving = h->cfg.include_moving_boundary;
     a.eqbc = h->cfg.include_equilibrium_bc;

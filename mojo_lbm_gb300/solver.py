@@ -93,6 +93,12 @@ class Solver:
         check(self._lib.lbm_compute_rho_u(self._h, ptr(rho), ptr(u), ptr(f), ptr(bc), ptr(flags),
                                           int(bool(after_odd_step)), stream_ptr(stream)))
 
+    def q_criterion(self, q, f, bc, flags, u, tau: float, after_odd_step: bool = False, stream=None) -> None:
+        """calculate_Q_criterion (output/Q_criterion.mojo:90-216) into q ([nx, ny, nz]); u is the
+        [D, nx, ny, nz] velocity of compute_rho_u for the same state."""
+        check(self._lib.lbm_q_criterion(self._h, ptr(q), ptr(f), ptr(bc), ptr(flags), ptr(u), float(tau),
+                                        int(bool(after_odd_step)), stream_ptr(stream)))
+
     def mass_momentum(self, f, flags, after_odd_step: bool = False, stream=None) -> tuple[float, ...]:
         out = (C.c_double * 4)()
         check(self._lib.lbm_reduce_mass_momentum(self._h, ptr(f), ptr(flags), int(bool(after_odd_step)), out,

@@ -47,6 +47,7 @@ def lib() -> C.CDLL:
         h.oracle_lattice.argtypes = [i32, vp, vp, vp]
         h.oracle_max_threads.restype = i32
         h.oracle_set_closure.argtypes = [vp]
+        h.oracle_q_criterion.argtypes = [vp, vp, i32, vp, vp, vp, vp, f64, i32, vp]
         h.oracle_closure_eval.argtypes = [i32, i32, i64, vp, vp, vp, vp, vp, vp, vp]
         _lib = h
     return _lib
@@ -97,6 +98,18 @@ def rho_u(cfg, grid, prec: int, f, bc, flags, after_odd: bool = False):
     g = grid.to_c()
     lib().oracle_rho_u(_cfg(cfg), C.byref(g), prec, _p(f), _p(bc), _p(flags), _p(rho), _p(u), int(bool(after_odd)))
     return rho.reshape(grid.shape), u.reshape((D,) + grid.shape)
+
+
+def q_criterion(cfg, grid, prec: int, f, bc, flags, u, tau: float, after_odd: bool = False, fill=np.nan):
+    """Q-criterion [nx, ny, nz] of the state f with velocity u ([D, nx, ny, nz], e.g. from
+    rho_u); cells with a raw SOLID flag keep `fill`."""
+    dt = np.float64 if prec == 64 else np.float32
+    q = np.full(grid.num_points, fill, dtype=dt)
+    u = np.ascontiguousarray(u, dtype=dt)
+    g = grid.to_c()
+    lib().oracle_q_criterion(_cfg(cfg), C.byref(g), prec, _p(f), _p(bc), _p(flags), _p(u), float(tau),
+                             int(bool(after_odd)), _p(q))
+    return q.reshape(grid.shape)
 
 
 def links(cfg, grid, prec: int, f, force, ids, dirs, dists, method: int, compute_force: bool, q_clamp: float):

@@ -626,9 +626,45 @@ void gather_post(const LatticeDef& L, const Layout& lay, const S* f, int64_t x, 
 }
 
 /* calculate_rho_and_velocity (output/velocity.mojo:25-125): stream + BC, then moments. */
-template <class R, class S>
+/* get_velocity_gradient (kernels/utils/finite_difference.mojo:14-140) with dx = 1: component
+ * comp of u ([D][nx][ny][nz]) along axis at p.  Spacing 1 to an in-grid neighbour, 1/2 when it is
+ * SOLID (raw compare), 0 (no term) outside the grid; weights 1 - own spacing / total. */
+template <class R>
+R velocity_gradient(const Layout& lay, const uint8_t* flags, const R* u, const int64_t* p, int comp, int axis) {
+    const int64_t n[3] = {lay.nx, lay.ny, lay.nz};
+    const int64_t N = lay.nx * lay.ny * lay.nz;
+    auto U = [&](const int64_t* q) { return u[N * comp + (q[0] * lay.ny + q[1]) * lay.nz + q[2]]; };
+    const R u2 = U(p);
+    R lg = 0, ldx = 0, rg = 0, rdx = 0;
+    int64_t a[3] = {p[0], p[1], p[2]};
+    a[axis] = p[axis] - 1;
+    const bool vl = a[axis] >= 0;
+    if (vl) {
+        const R gdx = flags[lay.flag(a[0], a[1], a[2])] == LBM_FLAG_SOLID ? (R)0.5 : (R)1;
+        lg = (u2 - U(a)) * ((R)1 / gdx);
+        ldx = gdx;
+    }
+    a[axis] = p[axis] + 1;
+    const bool vr = a[axis] < n[axis];
+    if (vr) {
+        const R gdx = flags[lay.flag(a[0], a[1], a[2])] == LBM_FLAG_SOLID ? (R)0.5 : (R)1;
+        rg = (U(a) - u2) * ((R)1 / gdx);
+        rdx = gdx;
+    }
+    if (!vl && !vr) return 0;
+    const R total = ldx + rdx;
+    const R lw = (R)1 - ldx / total;
+    const R rw = (R)1 - lw;
+    return rg * rw + lg * lw;
+}
+
+/* QCRIT: calculate_Q_criterion (output/Q_criterion.mojo:90-216) into q_out ([nx][ny][nz]) from
+ * the same streamed populations, u_in ([D][nx][ny][nz]) and tau; cells with a raw SOLID flag are
+ * skipped. */
+template <class R, class S, bool QCRIT = false>
 void run_rho_u(const lbm_config_t* cfg, const lbm_grid_t* g, const void* fv, const void* bcv,
-               const uint8_t* flags, void* rho_out, void* u_out, int after_odd) {
+               const uint8_t* flags, void* rho_out, void* u_out, int after_odd, const void* u_in = nullptr,
+               void* q_out = nullptr, double tau = 1.0) {
     const LatticeDef L = make_lattice(g->lattice);
     const Layout lay = make_layout(g);
     lbm_config_t c2 = *cfg;
@@ -644,8 +680,10 @@ void run_rho_u(const lbm_config_t* cfg, const lbm_grid_t* g, const void* fv, con
         const int64_t r = (x * lay.ny + y) * lay.nz + z; /* row-major [nx, ny, nz] */
         const uint8_t flag = flags[lay.flag(x, y, z)];
         if (flag == LBM_FLAG_SOLID) {
-            for (int d = 0; d < D; ++d) uo[r + N * d] = bc[lay.cell(x, y, z, d, K)];
-            ro[r] = bc[lay.cell(x, y, z, D, K)];
+            if (!QCRIT) {
+                for (int d = 0; d < D; ++d) uo[r + N * d] = bc[lay.cell(x, y, z, d, K)];
+                ro[r] = bc[lay.cell(x, y, z, D, K)];
+            }
             continue;
         }
         /* stream + apply_boundary_conditions with the next step's load pattern */
@@ -709,8 +747,43 @@ void run_rho_u(const lbm_config_t* cfg, const lbm_grid_t* g, const void* fv, con
         const R rho = st.density(fq);
         R u[3];
         st.velocity(fq, rho, u);
-        ro[r] = rho;
-        for (int d = 0; d < D; ++d) uo[r + N * d] = u[d];
+        if (!QCRIT) {
+            ro[r] = rho;
+            for (int d = 0; d < D; ++d) uo[r + N * d] = u[d];
+            continue;
+        }
+        /* get_f_noneq_vec, get_non_eq_second_order_moment, get_strain_rate_tensor and its norm
+         * (kernels/utils/equilibrium.mojo:81-120, moment.mojo:111-215), as collide */
+        const R uu = st.udot(u);
+        R P[6];
+        for (int m = 0; m < st.nstress(); ++m) {
+            R acc = 0;
+            for (int q = 0; q < Q; ++q)
+                acc = acc + (fq[q] - st.feq(q, rho, u, uu, cfg->DDF_shift != 0)) * (R)L.c[q][st.sa(m)] * (R)L.c[q][st.sb(m)];
+            P[m] = acc;
+        }
+        const R kk = (R)-1 / ((R)2 * rho * st.cs2 * (R)tau);
+        R s2 = 0;
+        for (int m = 0; m < st.nstress(); ++m) {
+            const R Sm = P[m] * kk;
+            const R ss = Sm * Sm;
+            s2 = (st.sa(m) != st.sb(m)) ? s2 + ss * (R)2 : s2 + ss;
+        }
+        /* calculate_vorticity (Q_criterion.mojo:26-85), Vector.norm_squared (sequential sum) */
+        const R* ui = (const R*)u_in;
+        R w2 = 0;
+        if (D == 2) {
+            const R wz = velocity_gradient<R>(lay, flags, ui, p, 1, 0) - velocity_gradient<R>(lay, flags, ui, p, 0, 1);
+            w2 = w2 + wz * wz;
+        } else {
+            const R wx = velocity_gradient<R>(lay, flags, ui, p, 2, 1) - velocity_gradient<R>(lay, flags, ui, p, 1, 2);
+            const R wy = velocity_gradient<R>(lay, flags, ui, p, 0, 2) - velocity_gradient<R>(lay, flags, ui, p, 2, 0);
+            const R wz = velocity_gradient<R>(lay, flags, ui, p, 1, 0) - velocity_gradient<R>(lay, flags, ui, p, 0, 1);
+            w2 = w2 + wx * wx;
+            w2 = w2 + wy * wy;
+            w2 = w2 + wz * wz;
+        }
+        ((R*)q_out)[r] = (R)0.25 * w2 - (R)0.5 * s2;
     }
 }
 
@@ -828,6 +901,14 @@ int oracle_rho_u(const lbm_config_t* cfg, const lbm_grid_t* g, int prec, const v
     if (prec == 64) run_rho_u<double, double>(cfg, g, f, bc, flags, rho, u, after_odd);
     else if (cfg->use_float16c) run_rho_u<float, uint16_t>(cfg, g, f, bc, flags, rho, u, after_odd);
     else run_rho_u<float, float>(cfg, g, f, bc, flags, rho, u, after_odd);
+    return 0;
+}
+
+int oracle_q_criterion(const lbm_config_t* cfg, const lbm_grid_t* g, int prec, const void* f, const void* bc,
+                       const uint8_t* flags, const void* u, double tau, int after_odd, void* q) {
+    if (prec == 64) run_rho_u<double, double, true>(cfg, g, f, bc, flags, nullptr, nullptr, after_odd, u, q, tau);
+    else if (cfg->use_float16c) run_rho_u<float, uint16_t, true>(cfg, g, f, bc, flags, nullptr, nullptr, after_odd, u, q, tau);
+    else run_rho_u<float, float, true>(cfg, g, f, bc, flags, nullptr, nullptr, after_odd, u, q, tau);
     return 0;
 }
 
