@@ -459,6 +459,7 @@ def run_batch(args, wl: dict):
         return None
     peak, peak_kind = measured_peaks()
     achieved = 72 * N / (launch_ms * 1e-3) / 1e9
+    traffic, traffic_src = profiled_traffic(args.workload) if wl["batch"] == 512 else (None, None)
     line = {
         "metric": "D2Q9 MLUPs (batched domains)", "value": round(mlups, 2), "unit": "MLUPs", "n_gpus": world,
         "steps": K, "warmup": args.warmup, "ms_per_step": round(t_ms / K, 5), "higher_is_better": True,
@@ -467,9 +468,10 @@ def run_batch(args, wl: dict):
                    "tile": list(wl["tile"]), "tile_source": tile_source,
                    "l2": "no flush: 2 x %.2f GB of lattices exceed L2" % (N * 36 / 1e9)},
         "roofline": {"bound": "hbm", "achieved": round(achieved, 1), "peak": peak, "unit": "GB/s",
-                     "frac": round(achieved / peak, 4), "traffic": None,
+                     "frac": round(achieved / peak, 4), "traffic": traffic,
                      "note": f"72 B/update x {N} cells / median per-step CUDA-event time {launch_ms:.4f} ms "
-                             f"(persistent step + link kernel); peak {peak_kind}"},
+                             f"(persistent step + link kernel); peak {peak_kind}; traffic = ncu dram bytes per "
+                             f"launch ({traffic_src or 'no capture committed'}, scaled by cells)"},
         "cpu_baseline": None, "gpu_launches": 2 * K + 1, "clocks": clk,
     }
     print(json.dumps(line), flush=True)
