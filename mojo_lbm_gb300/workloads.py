@@ -52,7 +52,7 @@ class Channel:
 
 
 def channel_specs(n: int = 512, seed: int = 0, nx_range=(200, 800), granule=(16, 16)):
-    """(nx, ny, Re, y_offset) of the batch of BASELINE's fourth configuration: nx ~ U[200, 800],
+    """(nx, ny, Re, y_offset) of the batched cylinder-channel workload: nx ~ U[200, 800],
     ny = 0.41 nx, Re ~ U[20, 200], cylinder offset ~ U[-0.05, 0.05] ny; nx and ny rounded to
     multiples of the granule (so that every tile dividing the granule divides every domain)."""
     rng = np.random.default_rng(seed)

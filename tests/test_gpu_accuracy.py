@@ -1,6 +1,6 @@
 """Error of the GPU step against the float64 oracle, and mass drift, on 64^3 replicas of the
-D3Q19 float32 cavity (BASELINE configuration 2) and the D3Q27 KBC + Smagorinsky Float16C
-esoteric-pull cavity at Re = 10000 (configuration 3).
+D3Q19 SRT float32 lid-driven cube at Re = 100 and of the D3Q27 KBC + Smagorinsky Float16C
+esoteric-pull lid-driven cube at Re = 10000.
 
 The GPU runs in its own arithmetic and storage (float32, or Float16C codes with DDF shift); the
 oracle runs the same configuration in float64 arithmetic and float64 storage from the same
@@ -27,9 +27,9 @@ U = 0.1
 CASES = {
     # name: lattice, method, collision, LES, Float16C, Re, steps, (max |du|/U bound, rel L2 bound), mass bound
     # float32: the population error grows ~2e-8 per step with the float32 mass drift (rounding)
-    "config2_d3q19_srt_fp32": ("D3Q19", "db", "SRT", False, False, 100.0, 200, (5e-5, 1e-5), 1e-5),
+    "d3q19_srt_fp32_re100": ("D3Q19", "db", "SRT", False, False, 100.0, 200, (5e-5, 1e-5), 1e-5),
     # Float16C at tau = 0.5019: differences of one storage unit grow in the nearly inviscid flow
-    "config3_d3q27_kbc_les_f16c_eso": ("D3Q27", "eso", "KBC", True, True, 10000.0, 200, (5e-2, 2e-4), 1e-5),
+    "d3q27_kbc_les_f16c_eso_re1e4": ("D3Q27", "eso", "KBC", True, True, 10000.0, 200, (5e-2, 2e-4), 1e-5),
 }
 
 
