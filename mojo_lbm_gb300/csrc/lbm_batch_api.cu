@@ -214,6 +214,7 @@ lbm_status lbm_batch_set_domain(lbm_batch* b, int32_t i, void* f_a, void* f_b, f
     a.bc = bc;
     a.flags = flags;
     a.tau = tau;
+    a.inv_tau = 1.f / tau;  // IEEE float32 quotient, as the kernel would compute it
     a.Cs = b->cfg.Cs;
     a.trt_lambda = b->cfg.trt_lambda;
     a.ddf = b->cfg.DDF_shift;

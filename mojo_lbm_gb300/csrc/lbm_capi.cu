@@ -126,6 +126,7 @@ StepArgs step_args(const lbm_handle* h, const void* f_in, void* f_out, float* bc
     a.bc = bc;
     a.flags = flags;
     a.tau = tau;
+    a.inv_tau = 1.f / tau;  // IEEE float32 quotient, as the kernel would compute it
     a.Cs = h->cfg.Cs;
     a.trt_lambda = h->cfg.trt_lambda;
     a.ddf = h->cfg.DDF_shift;

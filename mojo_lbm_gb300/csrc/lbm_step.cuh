@@ -29,6 +29,7 @@ struct StepArgs {
     float* bc;
     const uint8_t* flags;
     float tau, Cs, trt_lambda;
+    float inv_tau;             // 1 / tau, rounded as the step would round it (SRT, RLBM without LES)
     int32_t ddf, moving, eqbc, cap_rho, cap_u, even;
     // block-per-tile path (256-cell tiles with power-of-two sides)
     const ClosureDev* closure; // learned LES closure's fragments (learned-closure kernels only)
@@ -297,7 +298,10 @@ __device__ __forceinline__ void collide(float (&f)[L::Q], float tau, const StepA
         }
         if constexpr (COLL == LBM_RLBM) {
             // RLBM (src/lbm/kernels/ops/collisions/collision.mojo:168-223)
-            const float one_m = 1.f - 1.f / tau_local;
+            float inv_tau;
+            if constexpr (LES) inv_tau = 1.f / tau_local;
+            else inv_tau = a.inv_tau;
+            const float one_m = 1.f - inv_tau;
             for_each_feq<L>(rho, u, uu, ddf, [&](auto qc, float e) {
                 constexpr int q = decltype(qc)::value;
                 float dot = 0.f;
@@ -333,7 +337,9 @@ __device__ __forceinline__ void collide(float (&f)[L::Q], float tau, const StepA
     }
     if constexpr (COLL == LBM_SRT) {
         // SRT (src/lbm/kernels/ops/collisions/collision.mojo:12-46)
-        const float inv_tau = 1.f / tau_local;
+        float inv_tau;
+        if constexpr (LES) inv_tau = 1.f / tau_local;
+        else inv_tau = a.inv_tau;  // the same IEEE quotient, taken once on the host
         for_each_feq<L>(rho, u, uu, ddf, [&](auto qc, float e) {
             constexpr int q = decltype(qc)::value;
             f[q] -= inv_tau * (f[q] - e);
@@ -728,8 +734,12 @@ __device__ __forceinline__ void tile_step(const StepArgs& a, const uint32_t tile
     }
 }
 
+#ifndef LBM_TILE_MIN_BLOCKS
+#define LBM_TILE_MIN_BLOCKS 5
+#endif
+
 template <class L, int METHOD, bool F16C, int COLL, int LES>
-__global__ void __launch_bounds__(256, (L::Q == 9) ? 5 : ((COLL == LBM_KBC || L::Q == 27) ? 3 : 4))
+__global__ void __launch_bounds__(256, (L::Q == 9) ? 5 : ((COLL == LBM_KBC || L::Q == 27) ? 3 : LBM_TILE_MIN_BLOCKS))
     step_kernel_tile(const StepArgs a) {
     static_assert(LES != kLesLearned, "the learned closure runs in step_kernel_learned");
     tile_step<L, METHOD, F16C, COLL, LES>(a, blockIdx.x, threadIdx.x);
