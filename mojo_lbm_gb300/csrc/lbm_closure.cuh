@@ -139,9 +139,6 @@ __device__ __forceinline__ void closure_features(const float* S, float s2, float
     x[7] = uu * r;
 }
 
-#ifndef LBM_CLOSURE_INTERLEAVE
-#define LBM_CLOSURE_INTERLEAVE 1
-#endif
 
 // Next layer's A fragments from a layer's accumulators: the accumulator layout of m16n8k16 (rows
 // g, g+8; columns 2t, 2t+1) is the A layout of the next k-slice, n-tiles 2kc and 2kc+1 forming
@@ -159,9 +156,9 @@ __device__ __forceinline__ void relu_to_a(const float (&h)[4][4], uint32_t (&a)[
 // nu_t of the calling lane's cell; every lane of the warp must call it.  c: the per-lane
 // fragments in shared memory; u: the uniform part; stage: 32 x uint4 of per-warp shared memory,
 // ys: 32 floats of per-warp shared memory.  in_range reports whether the normalised features
-// lie in the training range (finite weights assumed: lbm_set_closure rejects others).  With LBM_CLOSURE_INTERLEAVE both 16-cell row tiles of the warp go
-// through each layer together (every weight fragment read once, used twice); without, one row
-// tile after the other (fewer live registers).
+// lie in the training range (finite weights assumed: lbm_set_closure rejects others).  Both
+// 16-cell row tiles of the warp go through each layer together, so every weight fragment is read
+// once and used twice.
 __device__ __forceinline__ float warp_closure_nu(const ClosureDev* __restrict__ c, const ClosureUniform& u,
                                                  const float (&x)[8], uint4* stage, float* ys, bool& in_range) {
     const uint32_t lane = threadIdx.x & 31u, g = lane >> 2, t = lane & 3u;
@@ -180,7 +177,6 @@ __device__ __forceinline__ float warp_closure_nu(const ClosureDev* __restrict__ 
                              pack_bf16x2(xn[6], xn[7]));
     __syncwarp();
     const uint32_t* st = reinterpret_cast<const uint32_t*>(stage);
-#if LBM_CLOSURE_INTERLEAVE
     // Layer by layer, each layer's n-tiles in pairs: a pair (2kc, 2kc+1) of one layer's output is
     // k-slice kc of the next layer's input, so it is packed (ReLU, BF16) and consumed before the
     // next pair is computed.  16 accumulators live at a time instead of 32; the products and their
@@ -242,34 +238,6 @@ __device__ __forceinline__ float warp_closure_nu(const ClosureDev* __restrict__ 
             ys[16 * mt + g + 8] = y[mt][2];
         }
     }
-#else
-#pragma unroll 1
-    for (int mt = 0; mt < 2; ++mt) {
-        uint32_t a[2][4];
-        a[0][0] = st[(16 * mt + g) * 4 + t];
-        a[0][1] = st[(16 * mt + g + 8) * 4 + t];
-        a[0][2] = a[0][3] = 0u;
-        float h[4][4];
-#pragma unroll
-        for (int nt = 0; nt < 4; ++nt) mma_bf16_16816_bias(h[nt], a[0], c->w1f[nt][lane], c->b1q[nt][lane]);
-        relu_to_a(h, a);
-#pragma unroll
-        for (int nt = 0; nt < 4; ++nt) {
-            const uint4 ww = c->w2f[nt][lane];
-            mma_bf16_16816_bias(h[nt], a[0], make_uint2(ww.x, ww.y), c->b2q[nt][lane]);
-            mma_bf16_16816(h[nt], a[1], make_uint2(ww.z, ww.w));
-        }
-        relu_to_a(h, a);
-        float y[4];
-        const uint4 w3 = c->w3f[lane];
-        mma_bf16_16816_bias(y, a[0], make_uint2(w3.x, w3.y), c->b3q);
-        mma_bf16_16816(y, a[1], make_uint2(w3.z, w3.w));
-        if (t == 0u) {
-            ys[16 * mt + g] = y[0];
-            ys[16 * mt + g + 8] = y[2];
-        }
-    }
-#endif
     __syncwarp();
     const float yo = ys[lane];
     __syncwarp();  // stage / ys are reused by the next call
