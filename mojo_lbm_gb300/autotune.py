@@ -49,13 +49,14 @@ def best_tile(config, lattice, nx: int, ny: int, nz: int, *, flags=None, bc=None
     return _cache[ck]
 
 
-def batch_tile(shapes, build, *, steps: int = 50, stream=None):
+def batch_tile(shapes, build, *, steps: int = 50, stream=None, samples: int = 4):
     """Tile for a batch of domains of one lattice and configuration: the candidates that divide
-    every shape, each timed as a batch of the same total size made of replicas of the median-size
-    domain (one persistent launch per step, graph-replayed; the replicas share the domain's
-    read-only flags and boundary arrays).  build(shape, tile) returns (grid, config, flags, bc,
-    tau, links) with host arrays in that tile's layout, links None or (fluid ids, directions,
-    distances) for Bouzidi bounce-back.  Returns (tile, {tile: MLUPs})."""
+    every shape, each timed as a batch of about the same total size made of replicas of `samples`
+    domains at evenly spaced quantiles of the size distribution (one persistent launch per step,
+    graph-replayed).  Every replica has its own copy of its domain's flags and boundary values, so
+    their reads cost what they cost in the real batch.  build(shape, tile) returns (grid, config,
+    flags, bc, tau, links) with host arrays in that tile's layout, links None or (fluid ids,
+    directions, distances) for Bouzidi bounce-back.  Returns (tile, {tile: MLUPs})."""
     import numpy as np
     import torch
 
@@ -64,9 +65,11 @@ def batch_tile(shapes, build, *, steps: int = 50, stream=None):
     from .solver import Solver
     shapes = [tuple(int(v) for v in s) for s in shapes]
     cells = np.array([int(np.prod(s)) for s in shapes])
-    rep = shapes[int(np.argsort(cells)[len(cells) // 2])]
-    replicas = max(1, int(round(cells.sum() / np.prod(rep))))
-    grid0 = build(rep, rep)[0]
+    order = np.argsort(cells, kind="stable")
+    k = max(1, min(int(samples), len(shapes)))
+    picks = [shapes[int(order[int((2 * i + 1) * len(shapes) // (2 * k))])] for i in range(k)]
+    reps = [max(1, int(round(cells.sum() / k / np.prod(p)))) for p in picks]
+    grid0 = build(picks[0], picks[0])[0]
     common = None
     for s in shapes:
         c = set(candidates(grid0.lattice, *s))
@@ -75,23 +78,30 @@ def batch_tile(shapes, build, *, steps: int = 50, stream=None):
         raise ValueError("no 256-cell power-of-two tile divides every domain")
     timing = {}
     for tile in sorted(common):
-        grid, cfg, flags, bc, tau, links = build(rep, tile)
-        batch = BatchSolver([grid] * replicas, cfg)
-        fl, b = torch.from_numpy(flags).cuda(), torch.from_numpy(bc).cuda()
+        built = [build(p, tile) for p in picks]
+        cfg = built[0][1]
+        grids = [b[0] for b, r in zip(built, reps) for _ in range(r)]
+        batch = BatchSolver(grids, cfg)
         dtype = torch.int16 if cfg.use_float16c else torch.float32
-        f0 = torch.empty(grid.num_points * grid.Q, dtype=dtype, device="cuda")
-        Solver(grid, cfg).init_equilibrium(f0)
-        bufs = []
-        for i in range(replicas):
-            fa, fb = f0.clone(), f0.clone()
-            bufs.append((fa, fb))
-            batch.set_domain(i, fa, fb, b, fl, tau)
-        if links is not None:
-            ids, dirs, dists = (np.asarray(a) for a in links)
-            n = len(ids)
+        keep, links_all = [], []
+        i = 0
+        for (grid, _, flags, bc, tau, links), r in zip(built, reps):
+            f0 = torch.empty(grid.num_points * grid.Q, dtype=dtype, device="cuda")
+            Solver(grid, cfg).init_equilibrium(f0)
+            fl, b = torch.from_numpy(flags).cuda(), torch.from_numpy(bc).cuda()
+            for _ in range(r):
+                bufs = (f0.clone(), f0.clone(), b.clone(), fl.clone())
+                keep.append(bufs)
+                batch.set_domain(i, bufs[0], bufs[1], bufs[2], bufs[3], tau)
+                if links is not None:
+                    links_all.append((i, *(np.asarray(a) for a in links)))
+                i += 1
+        if links_all:
             t = lambda a, dt: torch.from_numpy(np.ascontiguousarray(a, dtype=dt)).cuda()  # noqa: E731
-            batch.set_links(t(np.repeat(np.arange(replicas), n), np.int32), t(np.tile(ids, replicas), np.int32),
-                            t(np.tile(dirs, replicas), np.int32), t(np.tile(dists, replicas), np.float32),
+            batch.set_links(t(np.concatenate([np.full(len(l[1]), l[0]) for l in links_all]), np.int32),
+                            t(np.concatenate([l[1] for l in links_all]), np.int32),
+                            t(np.concatenate([l[2] for l in links_all]), np.int32),
+                            t(np.concatenate([l[3] for l in links_all]), np.float32),
                             Bounceback_method.BOUZIDI, 0.0)
         batch.run(64, 0, stream)
         cur = torch.cuda.current_stream() if stream is None else stream
@@ -100,8 +110,8 @@ def batch_tile(shapes, build, *, steps: int = 50, stream=None):
         batch.run(steps, 0, stream)
         e1.record(cur)
         e1.synchronize()
-        timing[tile] = replicas * grid.num_points * steps / (e0.elapsed_time(e1) * 1e-3) / 1e6
+        timing[tile] = sum(g.num_points for g in grids) * steps / (e0.elapsed_time(e1) * 1e-3) / 1e6
         batch.close()
-        del bufs
+        del keep
         torch.cuda.empty_cache()
     return max(timing, key=timing.get), timing

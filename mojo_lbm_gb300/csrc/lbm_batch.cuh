@@ -59,25 +59,35 @@ __global__ void __launch_bounds__(256, (L::Q == 9) ? 5 : ((COLL == LBM_KBC || L:
     }
 }
 
-// tile_near of unit u from the tile_any bytes of its domain (one thread per unit).
-__device__ __forceinline__ void batch_near_unit(const BatchArgs& b, uint32_t u, const uint8_t* tile_any,
-                                                uint8_t* tile_near) {
+// warp_near bit of warp box i (unit i / 8, warp i % 8) from the box summaries of its domain
+// (one thread per box; 0 past the last box).
+__device__ __forceinline__ uint32_t batch_near_box(const BatchArgs& b, uint32_t i, const uint8_t* box_sum) {
+    const uint32_t u = i / kTileWarps;
+    if (u >= b.total_units) return 0u;
     const uint32_t d = find_domain(b.unit_begin, b.ndom, u);
-    const LayoutDesc& l = b.dom[d].lay;
     const uint32_t first = b.unit_begin[d];
-    tile_near[u] = tile_neighbourhood(tile_any + first, u - first, l.ntx, l.nty, l.ntz);
+    return warp_near(box_sum + (size_t)first * kTileWarps, b.dom[d].lay, u - first, i % kTileWarps);
 }
 
-// tile_any of every unit of every domain; one warp per unit.
-__device__ __forceinline__ void batch_summary_unit(const BatchArgs& b, uint32_t u, uint32_t lane,
-                                                   uint8_t* tile_any) {
-    const uint32_t d = find_domain(b.unit_begin, b.ndom, u);
+// Summary byte of warp box `box` of the batch (unit box / 8), recomputed only if its flags differ
+// from flags_seen (every box when force; flags_seen is indexed like the units: 256 cells per unit)
+// which takes the new flags; a recomputed box sets *changed = gen.  Called by the 32 lanes of one
+// warp.
+__device__ __forceinline__ void batch_box_summary(const BatchArgs& b, uint32_t box, uint8_t* box_sum,
+                                                  uint8_t* flags_seen, uint32_t* changed, uint32_t gen, int force) {
+    const uint32_t u = box / kTileWarps;
+    const bool valid = u < b.total_units;
+    const uint32_t d = valid ? find_domain(b.unit_begin, b.ndom, u) : 0u;
+    const uint32_t first = valid ? b.unit_begin[d] : 0u;
     const StepArgs& a = b.dom[d];
-    const uint8_t* p = a.flags + (size_t)(u - b.unit_begin[d]) * a.lay.T;
-    uint32_t any = 0;
-    for (uint32_t i = lane; i < a.lay.T; i += 32) any |= __ldg(p + i);
-    any = __reduce_or_sync(0xffffffffu, any);
-    if (lane == 0) tile_any[u] = any != 0u;
+    const uint32_t n = (u - first) * kTileCells + (box % kTileWarps) * 32u + (threadIdx.x & 31u);
+    const size_t seen = (size_t)u * kTileCells + (box % kTileWarps) * 32u + (threadIdx.x & 31u);
+    const uint8_t fl = valid ? __ldg(a.flags + n) : 0;
+    const bool diff = valid && (force || fl != flags_seen[seen]);
+    if (!__any_sync(0xffffffffu, diff)) return;  // warp-uniform
+    if (valid) flags_seen[seen] = fl;
+    warp_box_summary(valid ? a.flags : nullptr, n, valid, a.lay, box_sum + (size_t)first * kTileWarps);
+    if ((threadIdx.x & 31u) == 0u) *changed = gen;
 }
 
 struct BatchLinkArgs {

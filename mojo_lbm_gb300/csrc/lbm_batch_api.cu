@@ -34,8 +34,12 @@ struct lbm_batch {
     StepArgs* d_even = nullptr;
     StepArgs* d_odd = nullptr;
     uint32_t* d_begin = nullptr;
-    uint8_t* d_tile_any = nullptr;
+    uint8_t* d_box_sum = nullptr;
     uint8_t* d_tile_near = nullptr;
+    uint8_t* d_flags_seen = nullptr;  // the flags of the last summary, 256 cells per unit
+    uint32_t* d_changed = nullptr;    // summary round in which a box summary last changed
+    uint32_t summary_gen = 0;
+    bool summary_valid = false;
     bool dirty = true;
     BatchLaunch step = nullptr;
     // links (caller-owned device arrays, concatenated over domains)
@@ -71,15 +75,19 @@ void drop_graphs(lbm_batch* b) {
     b->graphs.clear();
 }
 
-__global__ void batch_near_kernel(const BatchArgs b, const uint8_t* tile_any, uint8_t* tile_near) {
-    const uint32_t u = blockIdx.x * blockDim.x + threadIdx.x;
-    if (u < b.total_units) batch_near_unit(b, u, tile_any, tile_near);
+// tile_near: per unit, the warp_near bits of its 8 warp boxes; one thread per box.  Skipped unless
+// a box summary changed in this round (*changed == gen).
+__global__ void batch_near_kernel(const BatchArgs b, const uint8_t* box_sum, uint8_t* tile_near,
+                                  const uint32_t* changed, uint32_t gen) {
+    if (*changed != gen) return;  // the same value for every thread
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    write_near_mask(i, b.total_units * kTileWarps, batch_near_box(b, i, box_sum), tile_near);
 }
 
-__global__ void batch_summary_kernel(const BatchArgs b, uint8_t* tile_any) {
-    const uint32_t warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, lane = threadIdx.x & 31;
-    if (warp >= b.total_units) return;
-    batch_summary_unit(b, warp, lane, tile_any);
+// The summary byte of every warp box of the batch whose flags changed; one warp per box.
+__global__ void batch_summary_kernel(const BatchArgs b, uint8_t* box_sum, uint8_t* flags_seen, uint32_t* changed,
+                                     uint32_t gen, int force) {
+    batch_box_summary(b, (blockIdx.x * blockDim.x + threadIdx.x) >> 5, box_sum, flags_seen, changed, gen, force);
 }
 
 lbm_status launch_links(lbm_batch* b, const StepArgs* dom, cudaStream_t s) {
@@ -141,7 +149,8 @@ lbm_status lbm_batch_create(const lbm_config_t* cfg, int32_t n_domains, const lb
         begin[i] = (uint32_t)units;
         units += (uint64_t)(N / kTileCells);
     }
-    if (units >= ((uint64_t)1 << 32)) return bfail(LBM_EINVAL, "too many tiles in the batch");
+    // (warp boxes, 8 per tile, are numbered in 32 bits)
+    if (units >= ((uint64_t)1 << 29)) return bfail(LBM_EINVAL, "too many tiles in the batch");
     begin[n_domains] = (uint32_t)units;
 
     lbm_batch* b = new lbm_batch();
@@ -163,8 +172,11 @@ lbm_status lbm_batch_create(const lbm_config_t* cfg, int32_t n_domains, const lb
     if (e == cudaSuccess) e = cudaMalloc(&b->d_even, sizeof(StepArgs) * n_domains);
     if (e == cudaSuccess) e = cudaMalloc(&b->d_odd, sizeof(StepArgs) * n_domains);
     if (e == cudaSuccess) e = cudaMalloc(&b->d_begin, sizeof(uint32_t) * (n_domains + 1));
-    if (e == cudaSuccess) e = cudaMalloc(&b->d_tile_any, units > 0 ? units : 1);
+    if (e == cudaSuccess) e = cudaMalloc(&b->d_box_sum, units > 0 ? units * kTileWarps : 1);
     if (e == cudaSuccess) e = cudaMalloc(&b->d_tile_near, units > 0 ? units : 1);
+    if (e == cudaSuccess) e = cudaMalloc(&b->d_flags_seen, units > 0 ? units * kTileCells : 1);
+    if (e == cudaSuccess) e = cudaMalloc(&b->d_changed, sizeof(uint32_t));
+    if (e == cudaSuccess) e = cudaMemset(b->d_changed, 0, sizeof(uint32_t));
     if (e == cudaSuccess)
         e = cudaMemcpy(b->d_begin, begin.data(), sizeof(uint32_t) * (n_domains + 1), cudaMemcpyHostToDevice);
     if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&b->capture_stream, cudaStreamNonBlocking);
@@ -182,8 +194,10 @@ lbm_status lbm_batch_destroy(lbm_batch* b) {
     cudaFree(b->d_even);
     cudaFree(b->d_odd);
     cudaFree(b->d_begin);
-    cudaFree(b->d_tile_any);
+    cudaFree(b->d_box_sum);
     cudaFree(b->d_tile_near);
+    cudaFree(b->d_flags_seen);
+    cudaFree(b->d_changed);
     if (b->capture_stream) cudaStreamDestroy(b->capture_stream);
     delete b;
     return LBM_OK;
@@ -283,10 +297,16 @@ lbm_status lbm_batch_run(lbm_batch* b, int64_t n_steps, int64_t first_step, void
         a.unit_begin = b->d_begin;
         a.ndom = (uint32_t)b->ndom;
         a.total_units = b->unit_begin.back();
-        const uint32_t blocks = (uint32_t)(((uint64_t)a.total_units * 32 + 255) / 256);
-        if (blocks) batch_summary_kernel<<<blocks, 256, 0, s>>>(a, b->d_tile_any);
+        const uint32_t nboxes = a.total_units * kTileWarps;  // < 2^32: fewer than 2^29 units
+        if (++b->summary_gen == 0u) ++b->summary_gen;  // 0 is the initial value of *d_changed
+        if (nboxes)
+            batch_summary_kernel<<<a.total_units, kTileCells, 0, s>>>(a, b->d_box_sum, b->d_flags_seen, b->d_changed,
+                                                                      b->summary_gen, b->summary_valid ? 0 : 1);
         LBM_BCK(cudaGetLastError());
-        if (blocks) batch_near_kernel<<<(a.total_units + 255u) / 256u, 256, 0, s>>>(a, b->d_tile_any, b->d_tile_near);
+        b->summary_valid = true;
+        if (nboxes)
+            batch_near_kernel<<<(nboxes + 255u) / 256u, 256, 0, s>>>(a, b->d_box_sum, b->d_tile_near, b->d_changed,
+                                                                    b->summary_gen);
         LBM_BCK(cudaGetLastError());
     }
     const int64_t chunk = 64;

@@ -29,26 +29,33 @@ using namespace lbm;
 
 namespace {
 
-// tile_any[t] = 1 if any flag of tile t is not FLUID; one warp per tile.
-__global__ void __launch_bounds__(256) tile_summary_kernel(const uint8_t* __restrict__ flags, uint32_t ntiles,
-                                                           uint32_t T, uint8_t* __restrict__ tile_any) {
-    const uint32_t warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, lane = threadIdx.x & 31;
-    if (warp >= ntiles) return;
-    const uint8_t* p = flags + (size_t)warp * T;
-    uint32_t any = 0;
-    for (uint32_t i = lane; i < T; i += 32) any |= __ldg(p + i);
-    any = __reduce_or_sync(0xffffffffu, any);
-    if (lane == 0) tile_any[warp] = any != 0u;
+// box_sum: the summary byte of every warp box (the 32 cells of one warp of a tile), recomputed only
+// for the boxes whose flags differ from flags_seen (the flags of the previous summary; every box
+// when force), which takes the new flags.  A recomputed box sets *changed = gen.
+__global__ void __launch_bounds__(256) box_summary_kernel(const uint8_t* __restrict__ flags,
+                                                          uint8_t* __restrict__ flags_seen, const LayoutDesc l,
+                                                          uint8_t* __restrict__ box_sum, uint32_t* changed,
+                                                          uint32_t gen, int force) {
+    const uint32_t n = blockIdx.x * blockDim.x + threadIdx.x;
+    const bool valid = n < l.ncells;
+    const uint8_t fl = valid ? __ldg(flags + n) : 0;
+    const bool diff = valid && (force || fl != flags_seen[n]);
+    if (!__any_sync(0xffffffffu, diff)) return;  // warp-uniform
+    if (valid) flags_seen[n] = fl;
+    warp_box_summary(flags, n, valid, l, box_sum);
+    if ((threadIdx.x & 31u) == 0u) *changed = gen;
 }
 
-// tile_near[t]: the neighbourhood of tile t holds a non-FLUID flag; one thread per tile.
-__global__ void __launch_bounds__(256) tile_near_kernel(const uint8_t* __restrict__ tile_any, uint32_t ntiles,
-                                                        int32_t ntx, int32_t nty, int32_t ntz,
-                                                        uint8_t* __restrict__ tile_near) {
-    const uint32_t t = blockIdx.x * blockDim.x + threadIdx.x;
-    if (t < ntiles) tile_near[t] = tile_neighbourhood(tile_any, t, ntx, nty, ntz);
+// tile_near: per tile, bit w = warp_near of its warp box w; one thread per warp box.  Skipped
+// (every thread returns) unless a box summary changed in this round (*changed == gen).
+__global__ void __launch_bounds__(256) tile_near_kernel(const uint8_t* __restrict__ box_sum, const LayoutDesc l,
+                                                        uint32_t nboxes, uint8_t* __restrict__ tile_near,
+                                                        const uint32_t* changed, uint32_t gen) {
+    if (*changed != gen) return;  // the same value for every thread
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    const uint32_t bit = i < nboxes ? warp_near(box_sum, l, i / kTileWarps, i % kTileWarps) : 0u;
+    write_near_mask(i, nboxes, bit, tile_near);
 }
-
 
 thread_local std::string g_err;
 
@@ -85,8 +92,12 @@ struct lbm_handle {
     StepLaunch step_tile;  // block-per-tile kernel, or null when the grid does not qualify
     StepLaunch step_learned;  // block-per-tile kernel with the learned closure (LES handles), or null
     int path;              // 0 auto, 1 generic only, 2 block-per-tile only
-    uint8_t* tile_any;     // per-tile "has a non-FLUID flag" bytes for the block-per-tile kernel
-    uint8_t* tile_near;    // the same over each tile's 3x3x3 neighbourhood
+    uint8_t* box_sum;      // per warp box (32 cells): summary byte (flags other than 0 inside, on faces)
+    uint8_t* flags_seen;   // the flags the summary was built from
+    uint32_t* changed;     // device word: summary round in which a box summary last changed
+    uint32_t summary_gen;  // summary rounds issued
+    int summary_valid;     // box_sum and flags_seen hold a complete summary
+    uint8_t* tile_near;    // per tile: warp_near bits of its 8 warp boxes (block-per-tile kernel)
     uint32_t ntiles;
     uint32_t mx, my, shx, shxy;
     int threads;
@@ -153,13 +164,19 @@ StepLaunch step_fn(const lbm_handle* h) {
     return h->closure_on ? h->step_learned : h->step_tile;
 }
 
-// Rebuilds the per-tile summary of `flags` for the block-per-tile kernel.
+// Brings the per-tile warp masks of the block-per-tile kernel up to date with `flags`: the boxes
+// whose flags changed since the previous call are summarised again, and the masks are rebuilt
+// only if one did (every step of a run with fixed flags costs one pass over the flags).
 lbm_status tile_summary(lbm_handle* h, const uint8_t* flags, cudaStream_t s) {
-    const uint32_t blocks = (h->ntiles * 32u + 255u) / 256u;
-    tile_summary_kernel<<<blocks, 256, 0, s>>>(flags, h->ntiles, h->lay.T, h->tile_any);
+    if (++h->summary_gen == 0u) ++h->summary_gen;  // 0 is the initial value of *changed
+    const uint32_t gen = h->summary_gen;
+    box_summary_kernel<<<h->ntiles, kTileCells, 0, s>>>(flags, h->flags_seen, h->lay, h->box_sum, h->changed, gen,
+                                                        h->summary_valid ? 0 : 1);
     LBM_CK(cudaGetLastError());
-    tile_near_kernel<<<(h->ntiles + 255u) / 256u, 256, 0, s>>>(h->tile_any, h->ntiles, h->lay.ntx, h->lay.nty,
-                                                                h->lay.ntz, h->tile_near);
+    h->summary_valid = 1;
+    const uint32_t nboxes = h->ntiles * kTileWarps;
+    tile_near_kernel<<<(nboxes + 255u) / 256u, 256, 0, s>>>(h->box_sum, h->lay, nboxes, h->tile_near, h->changed,
+                                                             gen);
     LBM_CK(cudaGetLastError());
     return LBM_OK;
 }
@@ -288,7 +305,11 @@ lbm_status lbm_create(const lbm_config_t* cfg, const lbm_grid_t* grid, lbm_handl
     h->my = (uint32_t)grid->ty - 1u;
     h->shx = (uint32_t)ilog2(grid->tx);
     h->shxy = (uint32_t)(ilog2(grid->tx) + ilog2(grid->ty));
-    h->tile_any = nullptr;
+    h->box_sum = nullptr;
+    h->flags_seen = nullptr;
+    h->changed = nullptr;
+    h->summary_gen = 0;
+    h->summary_valid = 0;
     h->tile_near = nullptr;
     h->threads = 256;
     h->scratch = nullptr;
@@ -300,7 +321,10 @@ lbm_status lbm_create(const lbm_config_t* cfg, const lbm_grid_t* grid, lbm_handl
     if (e == cudaSuccess) e = cudaDeviceGetAttribute(&h->sm_count, cudaDevAttrMultiProcessorCount, h->device);
     if (e == cudaSuccess) e = cudaMalloc(&h->scratch, sizeof(double) * (kReduceBlocks * kReduceWidth + 8));
     if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&h->capture_stream, cudaStreamNonBlocking);
-    if (e == cudaSuccess && h->step_tile) e = cudaMalloc(&h->tile_any, h->ntiles);
+    if (e == cudaSuccess && h->step_tile) e = cudaMalloc(&h->box_sum, (size_t)h->ntiles * kTileWarps);
+    if (e == cudaSuccess && h->step_tile) e = cudaMalloc(&h->flags_seen, (size_t)h->lay.ncells);
+    if (e == cudaSuccess && h->step_tile) e = cudaMalloc(&h->changed, sizeof(uint32_t));
+    if (e == cudaSuccess && h->step_tile) e = cudaMemset(h->changed, 0, sizeof(uint32_t));
     if (e == cudaSuccess && h->step_tile) e = cudaMalloc(&h->tile_near, h->ntiles);
     if (e != cudaSuccess) {
         lbm_destroy(h);
@@ -314,7 +338,9 @@ lbm_status lbm_destroy(lbm_handle* h) {
     if (!h) return LBM_OK;
     for (auto& kv : h->graphs) cudaGraphExecDestroy(kv.second);
     if (h->scratch) cudaFree(h->scratch);
-    if (h->tile_any) cudaFree(h->tile_any);
+    if (h->box_sum) cudaFree(h->box_sum);
+    if (h->flags_seen) cudaFree(h->flags_seen);
+    if (h->changed) cudaFree(h->changed);
     if (h->tile_near) cudaFree(h->tile_near);
     if (h->closure) cudaFree(h->closure);
     if (h->capture_stream) cudaStreamDestroy(h->capture_stream);

@@ -2,6 +2,7 @@
 // codec, the reference's tiled memory layout, and fast division for index decoding.
 #pragma once
 
+#include <cmath>
 #include <cstdint>
 #include <type_traits>
 #include <utility>
@@ -139,21 +140,51 @@ LBM_HD uint32_t f16c_scale_down_rz(float x) {
 #endif
 }
 
+// min(a, b, c) of IEEE minNum: a NaN operand is passed over (the result is NaN only if all are).
+LBM_HD float fmin3(float a, float b, float c) {
+#if defined(__CUDA_ARCH__)
+    float r;
+    asm("min.f32 %0, %1, %2, %3;" : "=f"(r) : "f"(a), "f"(b), "f"(c));
+    return r;
+#else
+    return fminf(fminf(a, b), c);
+#endif
+}
+
 // Encode, with the reference's rounding (add 0x800 to the float32 bits, round half up on the first
 // dropped bit, saturate to 0x7FFF, sign from the sum).  With y = |x| * 2^-112 rounded toward zero,
 // (bits(y) + 0x800) >> 12 is the code for every magnitude: in the normal range it is
 // (|b| >> 12) - (112 << 11) with b = bits(x) + 0x800; in the denormal range it is
 // floor(|x| * 2^25 + 1/2), which is the reference's (((0x7FF800 + m) >> (124 - e)) + 1) >> 1, and 0
-// below 2^-26.  NaN and infinity saturate.  The one case apart: a NaN whose mantissa is within 0x800
-// of all ones, where adding 0x800 carries into the sign bit and the reference's code is a signed
-// zero.  (Checked against the oracle's restatement of the reference for all 2^32 inputs.)
+// below 2^-26.
+// Saturation and NaN come from one three-way minimum taken before the scaling, of |x|, the
+// magnitude of the float whose bits are b, and kSat = 1.999267578125 (0x3FFFE800, the smallest
+// float with code 0x7FFF):
+//   - finite x: |float(b)| >= |x| (b is x's bits with 0x800 added to the magnitude) or float(b)
+//     is NaN, so the minimum is min(|x|, kSat), which saturates exactly where the code does;
+//   - infinity, and a NaN whose sum b is still NaN: the minimum is kSat, code 0x7FFF;
+//   - a NaN whose mantissa is within 0x800 of all ones: adding 0x800 carries into the sign bit, b
+//     is a denormal of at most 0x7FF ulps, the minimum scales to 0, and the code is the signed
+//     zero the reference gives.
+// (Checked against the oracle's restatement of the reference for all 2^32 inputs.)
+// (y + 0x800) >> 12 for y < 2^28, as the high word of the 64-bit y * 2^20 + 2^31: one wide
+// multiply-add on the FMA pipe in place of an add and a shift on the integer pipe.
+LBM_HD uint32_t round_shift12(uint32_t y) {
+#if defined(__CUDA_ARCH__)
+    uint64_t d;
+    asm("mad.wide.u32 %0, %1, %2, %3;" : "=l"(d) : "r"(y), "r"(1u << 20), "l"(0x80000000ull));
+    return (uint32_t)(d >> 32);
+#else
+    return (y + 0x00000800u) >> 12;
+#endif
+}
+
 LBM_HD uint32_t f16c_encode(float x) {
-    const uint32_t u = as_u32(x);
-    const uint32_t b = u + 0x00000800u;
-    uint32_t mag = (f16c_scale_down_rz(x) + 0x00000800u) >> 12;
-    mag = mag < 0x7FFFu ? mag : 0x7FFFu;
-    mag = (b & 0x7FFFFFFFu) < 0x00000800u ? 0u : mag;
-    return ((b & 0x80000000u) >> 16) | mag;
+    constexpr float kSat = 0x1.ffdp0f;
+    const uint32_t b = as_u32(x) + 0x00000800u;
+    const float m = fmin3(fabsf(x), fabsf(as_f32(b)), kSat);
+    const uint32_t mag = round_shift12(f16c_scale_down_rz(m));  // m <= kSat: the bits are below 2^27
+    return ((b >> 16) & 0x8000u) | mag;
 }
 
 // ---------------------------------------------------------------------------------------------

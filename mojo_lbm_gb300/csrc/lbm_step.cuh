@@ -34,8 +34,8 @@ struct StepArgs {
     // block-per-tile path (256-cell tiles with power-of-two sides)
     const ClosureDev* closure; // learned LES closure's fragments (learned-closure kernels only)
     ClosureUniform cl;         // and its warp-uniform part
-    const uint8_t* tile_near;  // per tile: 1 if a flag of the tile or of one of its 26 neighbours
-                               // (periodic) is not FLUID
+    const uint8_t* tile_near;  // per tile: bit w set if a cell of warp w or a cell it pulls from
+                               // holds a flag other than plain FLUID (warp_near)
     uint32_t mx, my, shx, shxy; // lx = t & mx, ly = (t >> shx) & my, lz = t >> shxy
 };
 
@@ -549,10 +549,9 @@ __global__ void __launch_bounds__(256) step_kernel(const StepArgs a) {
 // the in-tile coordinates are shifts of threadIdx, the tile coordinates are block-uniform, the
 // population offsets q*T are immediates and every neighbour offset is the own offset plus three
 // per-axis deltas computed once per thread (32-bit: requires Q*N < 2^31).  Before touching any
-// flag, a warp checks the tile-summary bytes of its tile and the 26 neighbouring tiles: when all
-// are zero every cell it owns is FLUID with FLUID neighbours, so the neighbour-flag gather and
-// every boundary branch are skipped (the common case away from walls).  Results are identical
-// to step_kernel.
+// flag, a warp reads its bit of the tile's mask byte: when it is clear, every cell the warp owns
+// and every cell it pulls from is plain FLUID, so the neighbour-flag gather and every boundary
+// branch are skipped (the common case away from walls).  Results are identical to step_kernel.
 // ---------------------------------------------------------------------------------------------
 constexpr uint32_t kTileCells = 256;
 
@@ -588,20 +587,97 @@ __device__ __forceinline__ void tile_deltas(const StepArgs& a, uint32_t bx, uint
     }
 }
 
-// 1 if tile t (tile grid ntx x nty x ntz, periodic) or one of its 26 neighbours holds a non-FLUID
-// flag, from the per-tile bytes `any`: the block-per-tile step skips every flag load when 0.
-__device__ __forceinline__ uint8_t tile_neighbourhood(const uint8_t* __restrict__ any, uint32_t t, int32_t ntx,
-                                                      int32_t nty, int32_t ntz) {
-    const int32_t bx = (int32_t)(t % (uint32_t)ntx), byz = (int32_t)(t / (uint32_t)ntx);
-    const int32_t by = byz % nty, bz = byz / nty;
+// Warp boxes.  Warp w of a 256-cell tile with power-of-two sides owns the cells tid = 32w..32w+31
+// of the tile, x fastest: a box of wx x wy x wz cells (wx = min(tx, 32), wy = min(ty, 32 / wx),
+// wz = 32 / (wx wy)), lane = ix + wx (iy + wy iz), and these boxes tile the whole grid.  A cell
+// pulls from its 26 neighbours at most one cell away: those outside its box lie on the faces of the
+// 26 neighbouring boxes that face it (on the intersection of two or three such faces for an edge
+// or corner neighbour).
+constexpr uint32_t kTileWarps = kTileCells / 32;
+
+// Summary byte of a warp box: bit 0 = a flag of its 32 cells is not 0; bits 1..6 = a flag of its
+// -x, +x, -y, +y, -z, +z face layer is not 0.
+constexpr uint32_t kBoxAny = 1u;
+__host__ __device__ constexpr uint32_t box_face_bit(int axis, int side) { return 1u << (1 + 2 * axis + (side > 0)); }
+
+// 1 if a cell of warp box (tile, w) or a cell it pulls from holds a flag byte other than 0, from the
+// box summaries (tile-major: index tile * 8 + w): the box's own bit 0, and for each of the 26
+// neighbouring boxes (periodic) the bits of its faces that face the box, all of them set.  When 0,
+// every cell of the warp is plain FLUID with plain FLUID pull neighbours, and the step skips every
+// flag load.  Exact for walls along the axes; elsewhere it may only report 1 where 0 would do.
+__device__ __forceinline__ uint32_t warp_near(const uint8_t* __restrict__ box_sum, const LayoutDesc& l,
+                                              uint32_t tile, uint32_t w) {
+    // tile sides and box sides are powers of two: shifts and masks; tile-grid sides are not
+    const int32_t tx = l.tx, ty = l.ty, tz = l.tz;
+    const int32_t wx = min(tx, 32), wy = min(ty, 32 / wx), wz = 32 / (wx * wy);
+    const int32_t stx = __ffs(tx) - 1, sty = __ffs(ty) - 1, stz = __ffs(tz) - 1;
+    const int32_t swx = __ffs(wx) - 1, swy = __ffs(wy) - 1, swz = __ffs(wz) - 1;
+    const uint32_t byz = l.d_ntx.div(tile);
+    const int32_t bx = (int32_t)(tile - byz * (uint32_t)l.ntx);
+    const int32_t bz = (int32_t)l.d_nty.div(byz), by = (int32_t)byz - bz * l.nty;
+    const int32_t t0 = (int32_t)(w * 32u);
+    const int32_t gx = ((bx << stx) + (t0 & (tx - 1))) >> swx;
+    const int32_t gy = ((by << sty) + ((t0 >> stx) & (ty - 1))) >> swy;
+    const int32_t gz = ((bz << stz) + (t0 >> (stx + sty))) >> swz;
+    const int32_t nbx = l.nx >> swx, nby = l.ny >> swy, nbz = l.nz >> swz;
     uint32_t r = 0u;
-    for (int32_t oz = -1; oz <= 1; ++oz)
-        for (int32_t oy = -1; oy <= 1; ++oy)
+#pragma unroll
+    for (int32_t oz = -1; oz <= 1; ++oz) {
+        int32_t z = gz + oz;
+        z = z < 0 ? nbz - 1 : (z >= nbz ? 0 : z);
+        z <<= swz;
+#pragma unroll
+        for (int32_t oy = -1; oy <= 1; ++oy) {
+            int32_t y = gy + oy;
+            y = y < 0 ? nby - 1 : (y >= nby ? 0 : y);
+            y <<= swy;
+            const int32_t tyz = l.ntx * ((y >> sty) + l.nty * (z >> stz));
+            const int32_t lyz = ((y & (ty - 1)) << stx) + ((z & (tz - 1)) << (stx + sty));
+#pragma unroll
             for (int32_t ox = -1; ox <= 1; ++ox) {
-                const int32_t x = (bx + ox + ntx) % ntx, y = (by + oy + nty) % nty, z = (bz + oz + ntz) % ntz;
-                r |= __ldg(any + (x + ntx * (y + nty * z)));
+                int32_t x = gx + ox;
+                x = x < 0 ? nbx - 1 : (x >= nbx ? 0 : x);
+                x <<= swx;
+                const uint32_t t = (uint32_t)((x >> stx) + tyz);
+                const uint32_t tid = (uint32_t)((x & (tx - 1)) + lyz);
+                const uint32_t sum = __ldg(box_sum + t * kTileWarps + (tid >> 5));
+                // the neighbour at offset -1 along an axis faces the box with its + face
+                uint32_t need = 0u;
+                if (ox) need |= box_face_bit(0, -ox);
+                if (oy) need |= box_face_bit(1, -oy);
+                if (oz) need |= box_face_bit(2, -oz);
+                if (!need) need = kBoxAny;
+                r |= (sum & need) == need;
             }
-    return r != 0u;
+        }
+    }
+    return r;
+}
+
+// Summary byte of the calling warp's box (cell index n of lane 0..31 in tile-major order; flags at
+// the same index; l: the layout, for the box shape).
+__device__ __forceinline__ void warp_box_summary(const uint8_t* __restrict__ flags, uint32_t n, bool valid,
+                                                 const LayoutDesc& l, uint8_t* __restrict__ box_sum) {
+    const uint32_t lane = threadIdx.x & 31u;
+    const int32_t wx = min(l.tx, 32), wy = min(l.ty, 32 / wx), wz = 32 / (wx * wy);
+    const int32_t ix = (int32_t)lane % wx, iy = ((int32_t)lane / wx) % wy, iz = (int32_t)lane / (wx * wy);
+    const bool f = valid && __ldg(flags + n) != 0;
+    uint32_t sum = __ballot_sync(0xffffffffu, f) != 0u ? kBoxAny : 0u;
+    const int32_t pos[3] = {ix, iy, iz}, ext[3] = {wx, wy, wz};
+#pragma unroll
+    for (int a = 0; a < 3; ++a) {
+        if (__ballot_sync(0xffffffffu, f && pos[a] == 0)) sum |= box_face_bit(a, -1);
+        if (__ballot_sync(0xffffffffu, f && pos[a] == ext[a] - 1)) sum |= box_face_bit(a, +1);
+    }
+    if (valid && lane == 0u) box_sum[n >> 5] = (uint8_t)sum;
+}
+
+// The per-tile mask byte from the warp_near bits of 8 consecutive threads (thread i: box i of the
+// tile-major numbering, i < nboxes); lanes 0, 8, 16, 24 write the byte of their tile.
+__device__ __forceinline__ void write_near_mask(uint32_t i, uint32_t nboxes, uint32_t bit, uint8_t* __restrict__ tile_near) {
+    const uint32_t m = __ballot_sync(0xffffffffu, i < nboxes && bit != 0u);
+    const uint32_t lane = threadIdx.x & 31u;
+    if (i < nboxes && (lane & 7u) == 0u) tile_near[i / kTileWarps] = (uint8_t)(m >> lane);
 }
 
 // The per-thread body of the block-per-tile step: thread `tid` of the CTA that owns tile `tile`.
@@ -624,10 +700,10 @@ __device__ __forceinline__ void tile_step(const StepArgs& a, const uint32_t tile
     const uint32_t bz = a.lay.d_nty.div(byz);
     const uint32_t by = byz - bz * (uint32_t)a.lay.nty;
 
-    // ---- is the tile's neighbourhood all FLUID?  (one byte per tile, block-uniform)
-    // (the vote makes the value warp-uniform to the compiler: uniform branches below)
-    const bool clean =
-        __all_sync(0xffffffffu, (near >= 0 ? (uint32_t)near : (uint32_t)__ldg(a.tile_near + tile)) == 0u);
+    // ---- are this warp's cells and their pull neighbours all plain FLUID?  (bit w of the tile's
+    // mask byte; the vote makes the value warp-uniform to the compiler: uniform branches below)
+    const uint32_t mask = near >= 0 ? (uint32_t)near : (uint32_t)__ldg(a.tile_near + tile);
+    const bool clean = __all_sync(0xffffffffu, ((mask >> (tid >> 5)) & 1u) == 0u);
 
     uint8_t flag = 0;
     bool active = true;

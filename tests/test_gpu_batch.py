@@ -87,3 +87,38 @@ def test_batch_rejects_unsupported_tiles():
     from mojo_lbm_gb300 import LBM_Grid, get_D2Q9
     with pytest.raises(Exception, match="256-cell"):
         BatchSolver([LBM_Grid(get_D2Q9(), 30, 20, 1, (10, 5, 1))], LBM_Config())
+
+
+def test_batch_flags_changing_between_runs():
+    """Flags rewritten in place between batched runs (a block of SOLID cells appears in one
+    channel, then the original flags return): the batch's warp masks follow each change, and the
+    batch still equals the single-domain steps bit for bit."""
+    chans = _channels()
+    cfg = chans[0].cfg
+    batch = BatchSolver([c.grid for c in chans], cfg)
+    bufs = []
+    for i, ch in enumerate(chans):
+        fa = _f0(ch, cfg)
+        bufs.append((fa, fa.clone(), torch.from_numpy(ch.bc).cuda(), torch.from_numpy(ch.flags).cuda()))
+        batch.set_domain(i, *bufs[i], ch.tau)
+    ref = [(a.clone(), b.clone()) for a, b, _, _ in bufs]
+    solvers = [Solver(ch.grid, cfg) for ch in chans]
+    blocked = chans[2].flags.copy()
+    blocked[300:340] = 1  # SOLID cells in the interior of the third channel (its second tile)
+    T, K = 256, 3  # the block's boundary values (read by the moving wall at a SOLID cell) are numbers
+    cells = np.arange(300, 340)
+    assert np.isfinite(chans[2].bc[(cells % T)[:, None] + T * (np.arange(K) + K * (cells // T)[:, None])]).all()
+    plan = [(None, 3), (blocked, 4), (None, 64), (blocked, 1)]
+    k = 0
+    for new_flags, n in plan:
+        bufs[2][3].copy_(torch.from_numpy(chans[2].flags if new_flags is None else new_flags))
+        batch.run(n, k)
+        for i, ch in enumerate(chans):
+            fa, fb = ref[i]
+            for j in range(n):
+                src, dst = (fa, fb) if (k + j) % 2 == 0 else (fb, fa)
+                solvers[i].double_buffer_step(dst, src, bufs[i][2], bufs[i][3], ch.tau)
+        k += n
+    torch.cuda.synchronize()
+    for i in range(len(chans)):
+        assert torch.equal(bufs[i][0], ref[i][0]) and torch.equal(bufs[i][1], ref[i][1]), f"domain {i} differs"

@@ -152,6 +152,86 @@ def test_tile_kernel_with_clean_tiles(lat, meth, f16):
     assert_close(got, ref, cfg, "periodic")
 
 
+# Tile shapes whose warps own boxes of different shape (x rows of 32, slabs, columns): 256 x 1 and
+# 32 x 8 -> 32 x 1 boxes; 16 x 16 -> 16 x 2; 4 x 64 -> 4 x 8; 1 x 256 -> 1 x 32; 8 x 8 x 4 -> 8 x 4 x 1;
+# 2 x 4 x 32 -> 2 x 4 x 4; 1 x 16 x 16 -> 1 x 16 x 2; 1 x 1 x 256 -> 1 x 1 x 32.
+WARP_BOX_TILES = {"D2Q9": ((256, 256, 1), [(256, 1, 1), (32, 8, 1), (16, 16, 1), (4, 64, 1), (1, 256, 1)]),
+                  "D3Q19": ((64, 32, 32), [(32, 8, 1), (8, 8, 4), (2, 4, 32), (1, 16, 16), (64, 2, 2)]),
+                  "D3Q27": ((16, 16, 256), [(4, 8, 8), (16, 4, 4), (1, 1, 256)])}
+WARP_BOX_CASES = [(lat, t, meth, f16) for lat, (_, ts) in WARP_BOX_TILES.items() for t in ts
+                  for meth in ("db", "eso") for f16 in (False, True)]
+
+
+@pytest.mark.parametrize("lat,tile,meth,f16", WARP_BOX_CASES,
+                         ids=[f"{c[0]}-{'x'.join(map(str, c[1]))}-{c[2]}-{'f16c' if c[3] else 'fp32'}"
+                              for c in WARP_BOX_CASES])
+def test_sparse_flags_warp_masks(lat, tile, meth, f16):
+    """Isolated flags of every kind in an otherwise plain-FLUID periodic grid: only the warps whose
+    32 cells or 1-cell halo (across warp-box, tile and periodic edges) hold one take the flag
+    branch of the block-per-tile kernel, the rest the fast branch; bit-exact against the oracle."""
+    shape = WARP_BOX_TILES[lat][0]
+    grid = make_grid(lat, shape, tile)
+    rng = np.random.default_rng(zlib.crc32(f"sparse/{lat}/{tile}/{meth}/{f16}".encode()))
+    m = LBM_method.DOUBLE_BUFFER if meth == "db" else LBM_method.ESOTERIC_PULL
+    cfg = LBM_Config(m, BCs={Flags.EQUILIBRIUM}, DDF_shift=f16, use_float16c=f16, capture_density=True,
+                     capture_velocity=True)
+    flags, bc = mixed_flags(grid, rng)
+    flags[rng.random(flags.size) >= 0.004] = 0
+    f0 = initial_f(grid, cfg, rng)
+    got, ref, bc_gpu, bc_ref = run_both(grid, cfg, flags, bc, f0, 0.8, 4, path=2)
+    assert_close(got, ref, cfg, f"sparse flags, tile {tile}")
+    assert np.array_equal(bc_gpu.view(np.uint32), bc_ref.view(np.uint32))
+
+
+@pytest.mark.parametrize("f16", [False, True])
+def test_flags_changing_between_steps(f16):
+    """One handle stepped with a flag field that changes between calls (rewritten in place, and a
+    second buffer), by single steps and by graph-replayed runs: the block-per-tile kernel's warp
+    masks follow every change; bit-exact against the oracle."""
+    grid = make_grid("D3Q19", (32, 32, 16), (8, 8, 4))
+    cfg = LBM_Config(LBM_method.DOUBLE_BUFFER, BCs={Flags.EQUILIBRIUM}, DDF_shift=f16, use_float16c=f16,
+                     capture_density=True, capture_velocity=True)
+    rng = np.random.default_rng(77)
+    fl_a, bc = mixed_flags(grid, rng)
+    fl_a[rng.random(fl_a.size) >= 0.01] = 0
+    # fixed boundary values everywhere (no free NaN components): a cell that is EQUILIBRIUM in one
+    # field is a wall in another, and a wall's velocity and density must be numbers
+    comp = (np.arange(bc.size) // grid.layouts.T) % (grid.D + 1)
+    bc[np.isnan(bc)] = np.where(comp[np.isnan(bc)] == grid.D, 1.0, 0.0)
+    fl_b, _ = ldc_flags(grid, cfg, 0.1)
+    fl_c = np.zeros_like(fl_a)
+    f0 = initial_f(grid, cfg, rng)
+    solver = Solver(grid, cfg)
+    assert solver.kernel_path == 2
+    fa, fb, bct = to_dev(f0), to_dev(f0), to_dev(bc)
+    flt, flt2 = to_dev(fl_a), to_dev(fl_b)
+    f, f2, bco = f0.copy(), f0.copy(), bc.copy()
+    k = 0
+    # (flag field, buffer: 0 = the first buffer, rewritten in place with the field; 1 = a second
+    # buffer holding fl_b, steps, by graph-replayed run)
+    plan = [(fl_a, 0, 2, False), (fl_b, 1, 3, False), (fl_a, 0, 1, False), (fl_c, 0, 2, False),
+            (fl_b, 1, 64, True), (fl_a, 0, 64, True), (fl_b, 0, 1, False), (fl_b, 1, 1, False)]
+    for host, which, n, by_run in plan:
+        if which == 0:
+            flt.copy_(to_dev(host))
+        dev = flt if which == 0 else flt2
+        if by_run:
+            solver.run(fa, fb, bct, dev, 0.8, n, k)
+        else:
+            for j in range(n):
+                src, dst = (fa, fb) if (k + j) % 2 == 0 else (fb, fa)
+                solver.double_buffer_step(dst, src, bct, dev, 0.8)
+        for _ in range(n):
+            oracle.step(cfg, grid, 32, f2, f, bco, host, 0.8)
+            f, f2 = f2, f
+        k += n
+    torch.cuda.synchronize()
+    got = to_host(fa if k % 2 == 0 else fb, f0)
+    solver.close()
+    assert_close(got, f, cfg, "changing flags")
+    assert np.array_equal(bct.cpu().numpy().view(np.uint32), bco.view(np.uint32))
+
+
 def test_kernel_path_selection():
     assert Solver(make_grid("D3Q19", (16, 16, 8), (8, 8, 4)), LBM_Config()).kernel_path == 2
     assert Solver(make_grid("D3Q19", (18, 12, 10), (6, 4, 5)), LBM_Config()).kernel_path == 1
