@@ -54,6 +54,17 @@ WORKLOADS = {
                                        "Re ~ U[20,200], parabolic moving-wall inlet u_max=0.05, equilibrium outlet, "
                                        "Bouzidi links on the cylinder, FP32, one persistent launch per step"),
 }
+# The reference's published benchmark (README of JohnCSu/mojo_lbm): D3Q19 256^3, fully periodic, all
+# fluid, at rest, tau = 0.884 (benchmarks/D3.mojo:39-46), FP32 and Float16C + DDF shift; the MLUPs it
+# publishes for this configuration (on an RTX 2070 SUPER, one step per timed iteration) are the
+# vs_baseline denominators.
+for _f16, _pub in ((False, 2212.0), (True, 2776.0)):
+    WORKLOADS[f"periodic256_d3q19_{'f16c' if _f16 else 'fp32'}_rest"] = dict(
+        kind="rest", lattice="D3Q19", n=256, method="db", coll="SRT", les=False, f16=_f16, tau=0.884,
+        tile=(8, 8, 4), published_mlups=_pub,
+        desc="D3Q19 SRT periodic 256^3 at rest, tau=0.884, " + ("Float16C storage + DDF shift, FP32 math"
+                                                                if _f16 else "FP32/FP32")
+             + ", pull streaming (double buffer): the reference's published benchmark configuration")
 for _les in ("learned", "smagorinsky"):
     WORKLOADS[f"tgv256_d3q19_les_{_les}"] = dict(
         kind="tgv", lattice="D3Q19", n=256, method="db", coll="SRT", les=True, closure=_les, f16=False,
@@ -169,6 +180,14 @@ def build_case(wl: dict):
     if wl.get("kind") == "tgv":  # periodic, all fluid; tau from Re = u0 L / nu with L = n / (2 pi)
         cfg = LBM_Config(method, collision_op=wl["coll"], LES=True, include_moving_boundary=False)
         return grid, cfg, flags, bc, 3.0 * wl["U"] * (n / (2 * math.pi)) / wl["Re"] + 0.5
+    if wl.get("kind") == "rest":  # periodic, all fluid, rest equilibrium, fixed tau
+        cfg = LBM_Config(method, collision_op=wl["coll"], LES=wl["les"], DDF_shift=wl["f16"], use_float16c=wl["f16"],
+                         include_moving_boundary=False)
+        return grid, cfg, flags, bc, wl["tau"]
+    if wl.get("periodic"):  # diagnostic: the workload's kernel on a periodic box, no walls
+        cfg = LBM_Config(method, collision_op=wl["coll"], LES=wl["les"], DDF_shift=wl["f16"], use_float16c=wl["f16"],
+                         include_moving_boundary=False)
+        return grid, cfg, flags, bc, 3.0 * wl["U"] * (n - 1) / wl["Re"] + 0.5
     cfg = LBM_Config(method, collision_op=wl["coll"], LES=wl["les"], DDF_shift=wl["f16"], use_float16c=wl["f16"])
     for s in ("-Y", "+X", "-X", "+Z", "-Z"):
         preprocess.set_exterior_walls(grid, cfg, flags, bc, s, Flags.SOLID, [0.0] * D, 1.0)
@@ -233,13 +252,13 @@ def run_ours(args, wl: dict):
     bct = torch.from_numpy(bc).to(dev)
     flt = torch.from_numpy(flags).to(dev)
     closure = None
-    if wl.get("kind") == "tgv":
+    if wl.get("kind") == "tgv" or wl.get("periodic"):
         from mojo_lbm_gb300 import tgv
         from mojo_lbm_gb300.closure import LearnedClosure, set_closure
         u0, g0 = tgv.tgv_fields(grid.nx, wl["U"], seed=0, device=dev)
         solver.init_equilibrium(fa, 1.0, tau, u0, g0)
         del u0, g0
-        if wl["closure"] == "learned":
+        if wl.get("closure") == "learned":
             closure = LearnedClosure.load(CLOSURE_FILE, device=dev)
             set_closure(solver, closure)
     else:
@@ -353,9 +372,11 @@ def run_ours(args, wl: dict):
     line = {
         "metric": "D3Q19 MLUPs" if wl["lattice"] == "D3Q19" else f"{wl['lattice']} MLUPs",
         "value": round(mlups, 2), "unit": "MLUPs", "n_gpus": world, "steps": K, "warmup": args.warmup,
-        "ms_per_step": round(t_ms / K, 5), "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+        "ms_per_step": round(t_ms / K, 5), "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": round(mlups / wl["published_mlups"], 3) if wl.get("published_mlups") else None,
         "dtype": "f16c" if wl["f16"] else "f32",
-        "data": "synthetic (Taylor-Green vortex + seeded perturbation)" if wl.get("kind") == "tgv"
+        "data": "synthetic (Taylor-Green vortex + seeded perturbation)" if wl.get("kind") == "tgv" or wl.get("periodic")
+                else "synthetic (periodic box at rest)" if wl.get("kind") == "rest"
                 else "synthetic (lid-driven cavity from rest)",
         "config": {"workload": wl["desc"], "grid": [grid.nx, grid.ny, grid.nz], "tile": list(grid.tile_shape),
                    "tile_source": wl.get("tile_source", "default of the workload"),
@@ -539,7 +560,8 @@ def run_reference(args, wl: dict):
             "value": round(v, 3), "unit": "MLUPs", "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
             "ms_per_step": round(1e3 * t / len(times), 4), "higher_is_better": True, "scaling": "weak",
             "vs_baseline": None, "dtype": "f16c" if wl["f16"] else "f32",
-            "data": "synthetic (periodic box at rest)" if wl.get("kind") == "tgv" else "synthetic (lid-driven cavity)",
+            "data": "synthetic (periodic box at rest)" if wl.get("kind") in ("tgv", "rest")
+                    else "synthetic (lid-driven cavity from rest)",
             "config": {"workload": wl["desc"], "grid": [grid.nx, grid.ny, grid.nz], "tile": list(grid.tile_shape),
                        "step_sample": f"each step updates one slab of {slab} cells (1/64 of the grid)",
                        **({"reference_path": "Smagorinsky LES: the reference has no learned closure"}
@@ -568,6 +590,9 @@ def main(argv=None):
                     help="choose the layout's tile with the library's autotuner before the run")
     ap.add_argument("--no-autotune", action="store_true", help="keep the workload's default tile")
     ap.add_argument("--domains", type=int, default=0, help="domain count override of the batched workload")
+    ap.add_argument("--periodic", action="store_true",
+                    help="diagnostic: the cavity workload's kernel on a periodic box without walls, started from a "
+                         "perturbed Taylor-Green vortex (every warp on the block-per-tile kernel's fast branch)")
     args = ap.parse_args(argv)
     if args.warmup < 3:
         ap.error("--warmup must be at least 3")
@@ -580,6 +605,11 @@ def main(argv=None):
     if args.n:
         wl["n"] = args.n
         wl["desc"] = wl["desc"].replace("256^3", f"{args.n}^3")
+    if args.periodic:
+        if wl.get("kind") == "tgv" or wl.get("batch"):
+            ap.error("--periodic applies to the cavity workloads")
+        wl["periodic"] = True
+        wl["desc"] = "periodic-box diagnostic (no walls, perturbed Taylor-Green vortex) of: " + wl["desc"]
     if args.autotune and args.impl == "ours" and not wl.get("batch"):
         import torch
         from mojo_lbm_gb300 import autotune

@@ -69,25 +69,18 @@ __device__ __forceinline__ uint32_t batch_near_box(const BatchArgs& b, uint32_t 
     return warp_near(box_sum + (size_t)first * kTileWarps, b.dom[d].lay, u - first, i % kTileWarps);
 }
 
-// Summary byte of warp box `box` of the batch (unit box / 8), recomputed only if its flags differ
-// from flags_seen (every box when force; flags_seen is indexed like the units: 256 cells per unit)
-// which takes the new flags; a recomputed box sets *changed = gen.  Called by the 32 lanes of one
-// warp.
+// Brings the summary of warp box `box` of the batch (unit box / 8) up to date (update_box_summary;
+// flags_seen and box_sum hold 32 cells and one byte per box of the batch).  One thread per box.
 __device__ __forceinline__ void batch_box_summary(const BatchArgs& b, uint32_t box, uint8_t* box_sum,
                                                   uint8_t* flags_seen, uint32_t* changed, uint32_t gen, int force) {
     const uint32_t u = box / kTileWarps;
-    const bool valid = u < b.total_units;
-    const uint32_t d = valid ? find_domain(b.unit_begin, b.ndom, u) : 0u;
-    const uint32_t first = valid ? b.unit_begin[d] : 0u;
+    if (u >= b.total_units) return;
+    const uint32_t d = find_domain(b.unit_begin, b.ndom, u);
+    const uint32_t first = b.unit_begin[d];
     const StepArgs& a = b.dom[d];
-    const uint32_t n = (u - first) * kTileCells + (box % kTileWarps) * 32u + (threadIdx.x & 31u);
-    const size_t seen = (size_t)u * kTileCells + (box % kTileWarps) * 32u + (threadIdx.x & 31u);
-    const uint8_t fl = valid ? __ldg(a.flags + n) : 0;
-    const bool diff = valid && (force || fl != flags_seen[seen]);
-    if (!__any_sync(0xffffffffu, diff)) return;  // warp-uniform
-    if (valid) flags_seen[seen] = fl;
-    warp_box_summary(valid ? a.flags : nullptr, n, valid, a.lay, box_sum + (size_t)first * kTileWarps);
-    if ((threadIdx.x & 31u) == 0u) *changed = gen;
+    const uint32_t lb = box - first * kTileWarps;  // box index within the domain
+    update_box_summary(a.flags, lb, flags_seen + (size_t)first * kTileCells, box_sum + (size_t)first * kTileWarps, a.lay,
+                       changed, gen, force);
 }
 
 struct BatchLinkArgs {

@@ -84,10 +84,10 @@ __global__ void batch_near_kernel(const BatchArgs b, const uint8_t* box_sum, uin
     write_near_mask(i, b.total_units * kTileWarps, batch_near_box(b, i, box_sum), tile_near);
 }
 
-// The summary byte of every warp box of the batch whose flags changed; one warp per box.
+// The summary byte of every warp box of the batch whose flags changed; one thread per box.
 __global__ void batch_summary_kernel(const BatchArgs b, uint8_t* box_sum, uint8_t* flags_seen, uint32_t* changed,
                                      uint32_t gen, int force) {
-    batch_box_summary(b, (blockIdx.x * blockDim.x + threadIdx.x) >> 5, box_sum, flags_seen, changed, gen, force);
+    batch_box_summary(b, blockIdx.x * blockDim.x + threadIdx.x, box_sum, flags_seen, changed, gen, force);
 }
 
 lbm_status launch_links(lbm_batch* b, const StepArgs* dom, cudaStream_t s) {
@@ -300,8 +300,9 @@ lbm_status lbm_batch_run(lbm_batch* b, int64_t n_steps, int64_t first_step, void
         const uint32_t nboxes = a.total_units * kTileWarps;  // < 2^32: fewer than 2^29 units
         if (++b->summary_gen == 0u) ++b->summary_gen;  // 0 is the initial value of *d_changed
         if (nboxes)
-            batch_summary_kernel<<<a.total_units, kTileCells, 0, s>>>(a, b->d_box_sum, b->d_flags_seen, b->d_changed,
-                                                                      b->summary_gen, b->summary_valid ? 0 : 1);
+            batch_summary_kernel<<<(nboxes + 255u) / 256u, 256, 0, s>>>(a, b->d_box_sum, b->d_flags_seen,
+                                                                         b->d_changed, b->summary_gen,
+                                                                         b->summary_valid ? 0 : 1);
         LBM_BCK(cudaGetLastError());
         b->summary_valid = true;
         if (nboxes)

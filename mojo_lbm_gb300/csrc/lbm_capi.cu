@@ -31,19 +31,13 @@ namespace {
 
 // box_sum: the summary byte of every warp box (the 32 cells of one warp of a tile), recomputed only
 // for the boxes whose flags differ from flags_seen (the flags of the previous summary; every box
-// when force), which takes the new flags.  A recomputed box sets *changed = gen.
+// when force), which takes the new flags.  A recomputed box sets *changed = gen.  One thread per box.
 __global__ void __launch_bounds__(256) box_summary_kernel(const uint8_t* __restrict__ flags,
                                                           uint8_t* __restrict__ flags_seen, const LayoutDesc l,
                                                           uint8_t* __restrict__ box_sum, uint32_t* changed,
                                                           uint32_t gen, int force) {
-    const uint32_t n = blockIdx.x * blockDim.x + threadIdx.x;
-    const bool valid = n < l.ncells;
-    const uint8_t fl = valid ? __ldg(flags + n) : 0;
-    const bool diff = valid && (force || fl != flags_seen[n]);
-    if (!__any_sync(0xffffffffu, diff)) return;  // warp-uniform
-    if (valid) flags_seen[n] = fl;
-    warp_box_summary(flags, n, valid, l, box_sum);
-    if ((threadIdx.x & 31u) == 0u) *changed = gen;
+    const uint32_t box = blockIdx.x * blockDim.x + threadIdx.x;
+    if (box < l.ncells / 32u) update_box_summary(flags, box, flags_seen, box_sum, l, changed, gen, force);
 }
 
 // tile_near: per tile, bit w = warp_near of its warp box w; one thread per warp box.  Skipped
@@ -170,11 +164,11 @@ StepLaunch step_fn(const lbm_handle* h) {
 lbm_status tile_summary(lbm_handle* h, const uint8_t* flags, cudaStream_t s) {
     if (++h->summary_gen == 0u) ++h->summary_gen;  // 0 is the initial value of *changed
     const uint32_t gen = h->summary_gen;
-    box_summary_kernel<<<h->ntiles, kTileCells, 0, s>>>(flags, h->flags_seen, h->lay, h->box_sum, h->changed, gen,
-                                                        h->summary_valid ? 0 : 1);
+    const uint32_t nboxes = h->ntiles * kTileWarps;
+    box_summary_kernel<<<(nboxes + 255u) / 256u, 256, 0, s>>>(flags, h->flags_seen, h->lay, h->box_sum, h->changed,
+                                                              gen, h->summary_valid ? 0 : 1);
     LBM_CK(cudaGetLastError());
     h->summary_valid = 1;
-    const uint32_t nboxes = h->ntiles * kTileWarps;
     tile_near_kernel<<<(nboxes + 255u) / 256u, 256, 0, s>>>(h->box_sum, h->lay, nboxes, h->tile_near, h->changed,
                                                              gen);
     LBM_CK(cudaGetLastError());

@@ -232,6 +232,25 @@ def test_flags_changing_between_steps(f16):
     assert np.array_equal(bct.cpu().numpy().view(np.uint32), bco.view(np.uint32))
 
 
+@pytest.mark.parametrize("f16", [False, True])
+@pytest.mark.parametrize("kernel", ["generic", "tile"])
+def test_fluid_at_rest(f16, kernel):
+    """A periodic box at rest (zero momentum in every cell: the velocity's signed zeros are taken
+    without dividing), then one cell disturbed: bit-exact against the oracle."""
+    shape, tile = ((18, 12, 10), (6, 4, 5)) if kernel == "generic" else ((16, 16, 8), (8, 8, 4))
+    grid = make_grid("D3Q19", shape, tile)
+    cfg = LBM_Config(LBM_method.DOUBLE_BUFFER, DDF_shift=f16, use_float16c=f16, include_moving_boundary=False)
+    flags = np.zeros(grid.num_points, np.uint8)
+    bc = np.zeros(grid.num_points * 4, np.float32)
+    f0 = initial_f(grid, cfg, None)
+    got, ref, _, _ = run_both(grid, cfg, flags, bc, f0, 0.884, 4, path=1 if kernel == "generic" else 2)
+    assert_close(got, ref, cfg, "at rest")
+    f1 = f0.copy()
+    f1[grid.Q * 0 + 5] = oracle.f16c_encode(np.array([1e-3], np.float32))[0] if f16 else f1[5] + np.float32(1e-3)
+    got, ref, _, _ = run_both(grid, cfg, flags, bc, f1, 0.884, 6, path=1 if kernel == "generic" else 2)
+    assert_close(got, ref, cfg, "one cell disturbed")
+
+
 def test_kernel_path_selection():
     assert Solver(make_grid("D3Q19", (16, 16, 8), (8, 8, 4)), LBM_Config()).kernel_path == 2
     assert Solver(make_grid("D3Q19", (18, 12, 10), (6, 4, 5)), LBM_Config()).kernel_path == 1
