@@ -328,6 +328,36 @@ lbm_status lbm_autotune(const lbm_config_t* cfg, int32_t lattice, int32_t nx, in
                         const uint8_t* flags, const float* bc, int32_t choose_method, int32_t steps,
                         lbm_tune_result_t* out, void* stream);
 
+/* ---- wall and shape painting on the device ----
+ * Flags and boundary values painted straight into the caller's device arrays (grid layout), for
+ * set-ups too large to paint on the host (the 512^3 run, 512 batched channels).
+ *
+ * lbm_paint_wall replaces set_exterior_walls (src/lbm/preprocess/boundary_condition.mojo:78-183):
+ * every cell of the exterior face `side` (0..5 = "-X", "+X", "-Y", "+Y", "-Z", "+Z") gets flag
+ * boundary_type and bc (u[0..D-1], rho).  u = NULL leaves the velocity free (NaN); rho NaN leaves
+ * the density free.  It checks what the reference's _error_check checks (boundary_condition.mojo:
+ * 20-69) against cfg: the type must be FLUID, SOLID or (with include_equilibrium_bc) EQUILIBRIUM;
+ * u and rho cannot both be free; a given u has no NaN component; SOLID needs u and rho, and a
+ * non-zero u needs include_moving_boundary; EQUILIBRIUM with u needs rho.  Values are lattice
+ * units (a unit system converts on the host first).
+ * lbm_paint_wall_values replaces set_exterior_walls_with_func (:186-309): u_face holds D device
+ * arrays of the face's cell count, component-major, cells ordered by the face's first free axis
+ * fastest (y then z for an X face, x then z for Y, x then y for Z).
+ * lbm_paint_sphere / lbm_paint_box replace add_sphere / add_circle / add_box
+ * (src/lbm/geometry/primatives.mojo:110-240): SOLID in every cell of the reference's bounding box
+ * whose coordinate origin + n dx lies inside, tested in float32 in the reference's operation
+ * order (sphere: ((x-cx)^2 + (y-cy)^2) + (z-cz)^2 <= r^2; box: |coordinate - centre| <= half
+ * extent on every axis). */
+lbm_status lbm_paint_wall(const lbm_config_t* cfg, const lbm_grid_t* grid, uint8_t* flags, float* bc,
+                          int32_t side, uint8_t boundary_type, const float* u, float rho, void* stream);
+lbm_status lbm_paint_wall_values(const lbm_config_t* cfg, const lbm_grid_t* grid, uint8_t* flags, float* bc,
+                                 int32_t side, uint8_t boundary_type, const float* u_face, float rho,
+                                 void* stream);
+lbm_status lbm_paint_sphere(const lbm_grid_t* grid, uint8_t* flags, const float center[3], float radius,
+                            const float origin[3], float dx, void* stream);
+lbm_status lbm_paint_box(const lbm_grid_t* grid, uint8_t* flags, const float center[3], const float half[3],
+                         const float origin[3], float dx, void* stream);
+
 /* Float16C codec (src/utils/custom_fp.mojo:36-101) over device arrays. */
 lbm_status lbm_float16c_encode(const float* in, uint16_t* out, int64_t n, void* stream);
 lbm_status lbm_float16c_decode(const uint16_t* in, float* out, int64_t n, void* stream);

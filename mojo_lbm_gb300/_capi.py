@@ -94,6 +94,10 @@ SIGNATURES = {
     "lbm_tune_candidates": (_i32, [_i32, _i32, _i32, _i32, _vp, _i32]),
     "lbm_autotune": (_i32, [_CFG, _i32, _i32, _i32, _i32, _vp, _vp, _i32, _i32, C.POINTER(lbm_tune_result_t),
                             _vp]),
+    "lbm_paint_wall": (_i32, [_CFG, _GRID, _vp, _vp, _i32, C.c_uint8, C.POINTER(_f32), _f32, _vp]),
+    "lbm_paint_wall_values": (_i32, [_CFG, _GRID, _vp, _vp, _i32, C.c_uint8, _vp, _f32, _vp]),
+    "lbm_paint_sphere": (_i32, [_GRID, _vp, C.POINTER(_f32), _f32, C.POINTER(_f32), _f32, _vp]),
+    "lbm_paint_box": (_i32, [_GRID, _vp, C.POINTER(_f32), C.POINTER(_f32), C.POINTER(_f32), _f32, _vp]),
     "lbm_float16c_encode": (_i32, [_vp, _vp, _i64, _vp]),
     "lbm_float16c_decode": (_i32, [_vp, _vp, _i64, _vp]),
     "lbm_last_error": (C.c_char_p, []),

@@ -1,8 +1,10 @@
 """Immersed sphere/circle geometry and its bounce-back links
-(mirrors src/lbm/geometry/rigidSphere.mojo:14-170 and rigidstationary.mojo:21-169).
+(mirrors src/lbm/geometry/rigidSphere.mojo:14-170 and rigidstationary.mojo:21-169), and the solid
+shapes of src/lbm/geometry/primatives.mojo:17-266.
 
-Link discovery is host set-up (numpy); the bounce-back itself and the force sum run on the
-device through the library.
+Link discovery is host set-up (numpy); the bounce-back itself, the force sum and the shape
+painting (add_sphere / add_circle / add_box into a device flag tensor) run on the device through
+the library.
 """
 from __future__ import annotations
 
@@ -99,3 +101,86 @@ def get_rigid_sphere(grid, flags_host: np.ndarray, center, radius: float, device
     dists = get_q_for_sphere(xf[k_idx], xs[k_idx, q_idx], c, radius) if len(k_idx) else np.zeros(0)
     uniq = fid[np.unique(k_idx)]
     return RigidStationaryObject(grid, uniq, ids, dirs, dists, device)
+
+
+def _f32x3(v, what: str):
+    import ctypes as C
+    v = [float(x) for x in v]
+    if len(v) != 3:
+        raise ValueError(f"{what} must be a list of 3 floats got a len of {len(v)} instead")
+    return (C.c_float * 3)(*v)
+
+
+def add_sphere(grid, flags, center, radius: float, stream=None) -> None:
+    """add_sphere (primatives.mojo:110-186): SOLID in every cell of the device flag tensor whose
+    coordinate lies within `radius` of `center` (physical units; float32 test over the reference's
+    bounding box)."""
+    import ctypes as C
+
+    from . import _capi
+    c = _f32x3(center, "centre")
+    _capi.check(_capi.lib().lbm_paint_sphere(C.byref(grid.to_c()), _capi.ptr(flags), c, float(radius),
+                                             _f32x3(grid.origin, "origin"), float(grid.dx), _capi.stream_ptr(stream)))
+
+
+def add_circle(grid, flags, center, radius: float, stream=None) -> None:
+    """add_circle (primatives.mojo:188-206): add_sphere on a 2D grid."""
+    if grid.D != 2:
+        raise ValueError("Circle only valid for 2D")
+    add_sphere(grid, flags, center, radius, stream)
+
+
+def add_box(grid, flags, center, box_radius, stream=None) -> None:
+    """add_box (primatives.mojo:210-245): SOLID in every cell of the device flag tensor within
+    box_radius (half extents) of center along every axis."""
+    import ctypes as C
+
+    from . import _capi
+    c = _f32x3(center, "centre")
+    h = _f32x3(box_radius, "lengths")
+    _capi.check(_capi.lib().lbm_paint_box(C.byref(grid.to_c()), _capi.ptr(flags), c, h,
+                                          _f32x3(grid.origin, "origin"), float(grid.dx), _capi.stream_ptr(stream)))
+
+
+def get_sphere_boundary_indices(grid, flags_host: np.ndarray, center, radius: float) -> np.ndarray:
+    """get_sphere_boundary_indices (primatives.mojo:17-104): marks the sphere SOLID in the host
+    flags and returns the flag-layout indices of the non-solid cells of its bounding box (one cell
+    wider) with a lattice neighbour inside it, in ascending order (the reference returns them in
+    the order of a hash set)."""
+    if len(center) != 3:
+        raise ValueError(f"centre must be a list of 3 floats got a len of {len(center)} instead")
+    f32 = np.float32
+    c = np.asarray(center, f32)
+    r = f32(radius)
+    dx = f32(grid.dx)
+    o = np.asarray(grid.origin, f32)
+    lo, hi = [], []
+    for i in range(3):
+        if i < grid.D:
+            n_min = max(0, int(np.floor((c[i] - r - o[i]) / dx)))
+            n_max = min(grid.shape[i], int(np.floor((c[i] + r - o[i]) / dx) + f32(1)))
+            lo.append(n_min)
+            hi.append(min(n_max + 1, grid.shape[i]))  # the reference's n_max + 1 can pass the grid's end
+        else:
+            lo.append(0)
+            hi.append(1)
+
+    def inside(n):
+        p = n.astype(f32) * dx + o
+        d = p - c
+        return ((d[..., 0] * d[..., 0] + d[..., 1] * d[..., 1]) + d[..., 2] * d[..., 2]) <= r * r
+
+    rng = [np.arange(lo[i], hi[i]) for i in range(3)]
+    X, Y, Z = np.meshgrid(*rng, indexing="ij")
+    n = np.stack([X.ravel(), Y.ravel(), Z.ravel()], -1)
+    ins = inside(n)
+    lay = grid.layouts
+    flags_host[lay.flag_offset(*n[ins].T)] = Flags.SOLID
+    cand = n[~ins]
+    cd = grid.lattice.directions.astype(np.int64)
+    hit = np.zeros(len(cand), bool)
+    for q in range(grid.Q):
+        m = cand.copy()
+        m[:, :grid.D] += cd[q]
+        hit |= inside(m)
+    return np.sort(lay.flag_offset(*cand[hit].T).astype(np.int64))
