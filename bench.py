@@ -310,17 +310,24 @@ def run_ours(args, wl: dict):
     bc_host = torch.from_numpy(bc).pin_memory()
     fl_host = torch.from_numpy(flags).pin_memory()
     out_host = torch.empty_like(f_host).pin_memory()
+
+    def e2e_pass(steps):
+        fa.copy_(f_host, non_blocking=True)
+        bct.copy_(bc_host, non_blocking=True)
+        flt.copy_(fl_host, non_blocking=True)
+        if wl["method"] == "db":
+            fb.copy_(fa)
+        solver.run(fa, fb, bct, flt, tau, steps, 0, stream)
+        out_host.copy_(fa if (steps % 2 == 0 or wl["method"] != "db") else fb, non_blocking=True)
+
+    # one untimed pass first: the first transfers from and to a freshly pinned buffer are slower
+    # (its pages are mapped for the copy engines then), which is set-up, not a step's cost
+    e2e_pass(64)
     barrier(world)
     torch.cuda.synchronize(dev)
     h0, h1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
     h0.record(stream)
-    fa.copy_(f_host, non_blocking=True)
-    bct.copy_(bc_host, non_blocking=True)
-    flt.copy_(fl_host, non_blocking=True)
-    if wl["method"] == "db":
-        fb.copy_(fa)
-    solver.run(fa, fb, bct, flt, tau, K, 0, stream)
-    out_host.copy_(fa if (K % 2 == 0 or wl["method"] != "db") else fb, non_blocking=True)
+    e2e_pass(K)
     h1.record(stream)
     torch.cuda.synchronize(dev)
     barrier(world)
@@ -395,7 +402,7 @@ def run_ours(args, wl: dict):
         "e2e": {"value": round(e2e_mlups, 2), "unit": "MLUPs", "h2d_bytes_per_step": int(h2d / K),
                 "d2h_bytes_per_step": int(d2h / K),
                 "note": "Solver.run from pinned host buffers: upload of f, bc, flags and download of f inside the "
-                        f"timed region, amortised over the {K} steps"},
+                        f"timed region, amortised over the {K} steps (after one untimed pass of 64 steps)"},
         "gpu_launches": K + 2,
         "clocks": clk,
     }
@@ -485,18 +492,23 @@ def run_batch(args, wl: dict):
     hosts = [(torch.empty_like(fa, device="cpu").pin_memory().copy_(fa), torch.empty_like(bc, device="cpu").pin_memory()
               .copy_(bc), torch.empty_like(fl, device="cpu").pin_memory().copy_(fl), torch.empty_like(fa, device="cpu")
               .pin_memory()) for fa, fb, bc, fl in keep]
+
+    def e2e_pass(steps):
+        for (fa, fb, bc, fl), (fh, bh, flh, _) in zip(keep, hosts):
+            fa.copy_(fh, non_blocking=True)
+            fb.copy_(fa)
+            bc.copy_(bh, non_blocking=True)
+            fl.copy_(flh, non_blocking=True)
+        batch.run(steps, 0, stream)
+        for (fa, fb, bc, fl), (_, _, _, oh) in zip(keep, hosts):
+            oh.copy_(fa if steps % 2 == 0 else fb, non_blocking=True)
+
+    e2e_pass(64)  # untimed: maps the freshly pinned buffers for the copy engines
     barrier(world)
     torch.cuda.synchronize(dev)
     h0, h1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
     h0.record(stream)
-    for (fa, fb, bc, fl), (fh, bh, flh, _) in zip(keep, hosts):
-        fa.copy_(fh, non_blocking=True)
-        fb.copy_(fa)
-        bc.copy_(bh, non_blocking=True)
-        fl.copy_(flh, non_blocking=True)
-    batch.run(K, 0, stream)
-    for (fa, fb, bc, fl), (_, _, _, oh) in zip(keep, hosts):
-        oh.copy_(fa if K % 2 == 0 else fb, non_blocking=True)
+    e2e_pass(K)
     h1.record(stream)
     torch.cuda.synchronize(dev)
     barrier(world)
@@ -524,7 +536,8 @@ def run_batch(args, wl: dict):
         "e2e": {"value": round(e2e_units / (e2e_ms * 1e-3) / 1e6, 2), "unit": "MLUPs",
                 "h2d_bytes_per_step": int(h2d / K), "d2h_bytes_per_step": int(d2h / K),
                 "note": "BatchSolver.run with every domain's f, bc and flags uploaded from pinned host buffers and "
-                        f"every f downloaded inside the timed region, amortised over the {K} steps"},
+                        f"every f downloaded inside the timed region, amortised over the {K} steps (after one "
+                        "untimed pass of 64 steps)"},
         "gpu_launches": 2 * K + 2, "clocks": clk,
     }
     print(json.dumps(line), flush=True)
