@@ -234,12 +234,15 @@ def test_flags_changing_between_steps(f16):
 
 @pytest.mark.parametrize("f16", [False, True])
 @pytest.mark.parametrize("kernel", ["generic", "tile"])
-def test_fluid_at_rest(f16, kernel):
-    """A periodic box at rest (zero momentum in every cell: the velocity's signed zeros are taken
-    without dividing), then one cell disturbed: bit-exact against the oracle."""
+@pytest.mark.parametrize("coll,les", [("SRT", False), ("SRT", True), ("KBC", True), ("KBC", False)])
+def test_fluid_at_rest(f16, kernel, coll, les):
+    """A periodic box at rest (zero momentum in every cell: the velocity's signed zeros, KBC's zero
+    entropic terms and the zero strain norm are taken without dividing or a square root), then one
+    cell disturbed: bit-exact against the oracle."""
     shape, tile = ((18, 12, 10), (6, 4, 5)) if kernel == "generic" else ((16, 16, 8), (8, 8, 4))
     grid = make_grid("D3Q19", shape, tile)
-    cfg = LBM_Config(LBM_method.DOUBLE_BUFFER, DDF_shift=f16, use_float16c=f16, include_moving_boundary=False)
+    cfg = LBM_Config(LBM_method.DOUBLE_BUFFER, collision_op=coll, LES=les, DDF_shift=f16, use_float16c=f16,
+                     include_moving_boundary=False)
     flags = np.zeros(grid.num_points, np.uint8)
     bc = np.zeros(grid.num_points * 4, np.float32)
     f0 = initial_f(grid, cfg, None)
