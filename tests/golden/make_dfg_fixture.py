@@ -13,8 +13,8 @@ SRC = "benchmarks/Cylinder2D/CylinderFlow_Re20.mojo"
 OUT = Path(__file__).with_name("dfg_re20.json")
 
 
-def main() -> int:
-    text = (REF / SRC).read_text()
+def extract(text: str) -> dict:
+    """The fixture's content from the text of the reference's benchmark file."""
     cd = float(re.search(r"Drag coefficient:\s*Cd\s*=\s*([0-9.eE+-]+)", text).group(1))
     cl = float(re.search(r"Lift coefficient:\s*Cl\s*=\s*([0-9.eE+-]+)", text).group(1))
     # the recorded runs: a resolution header ("1024 x 256:"), optionally a collision name, then
@@ -35,8 +35,13 @@ def main() -> int:
             if not runs or runs[-1]["grid"] != res or runs[-1]["collision"] != coll or key in runs[-1]:
                 runs.append({"grid": res, "collision": coll})
             runs[-1][key] = float(m.group(2))
-    OUT.write_text(json.dumps({"source": SRC, "Cd": cd, "Cl": cl, "reference_runs": runs}, indent=1))
-    print(f"wrote {OUT}: Cd {cd}, Cl {cl}, {len(runs)} recorded runs")
+    return {"source": SRC, "Cd": cd, "Cl": cl, "reference_runs": runs}
+
+
+def main() -> int:
+    fix = extract((REF / SRC).read_text())
+    OUT.write_text(json.dumps(fix, indent=1))
+    print(f"wrote {OUT}: Cd {fix['Cd']}, Cl {fix['Cl']}, {len(fix['reference_runs'])} recorded runs")
     return 0
 
 

@@ -224,3 +224,23 @@ def test_ldc_re100_against_ghia_fixture():
     v_sim = np.interp(coord(xs[inner]), np.arange(N), vcl) / U
     assert np.abs(u_sim - us[inner]).max() < 0.03, np.c_[ys[inner], u_sim, us[inner]]
     assert np.abs(v_sim - vs[inner]).max() < 0.03, np.c_[xs[inner], v_sim, vs[inner]]
+
+
+# ---- the reference's DFG cylinder record (tests/golden/dfg_re20.json) --------------------------
+def test_dfg_fixture():
+    """The fixture holds the DFG targets and the reference's recorded drag for the resolutions the
+    GPU test runs; where the reference is present, extracting it again gives the same fixture."""
+    import importlib.util
+    import os
+    fix = json.loads((GOLDEN / "dfg_re20.json").read_text())
+    assert abs(fix["Cd"] - 5.58) < 0.01 and 0.0 < fix["Cl"] < 0.02
+    grids = {tuple(r["grid"]) for r in fix["reference_runs"]}
+    assert {(1024, 256), (2560, 512)} <= grids
+    for r in fix["reference_runs"]:
+        assert abs(r["drag"] - fix["Cd"]) / fix["Cd"] < 0.02
+    src = Path(os.environ.get("REF", "/root/reference")) / fix["source"]
+    if src.exists():
+        spec = importlib.util.spec_from_file_location("make_dfg_fixture", GOLDEN / "make_dfg_fixture.py")
+        mod = importlib.util.module_from_spec(spec)
+        spec.loader.exec_module(mod)
+        assert mod.extract(src.read_text()) == fix
