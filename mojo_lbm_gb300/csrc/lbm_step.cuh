@@ -338,10 +338,14 @@ __device__ __forceinline__ void collide(float (&f)[L::Q], float tau, const StepA
             // adding a zero leaves these sums, which start at +0, unchanged.  Such terms are skipped
             // rather than divided: a zero numerator sends IEEE division to its special-case path, a
             // third of its usual rate on this GPU.  (dh = 0 also means ds is finite.)
+            // dh of every direction waits in shared memory (lane-fastest) for the update, which
+            // then needs no third f_eq per direction
+            __shared__ float dh_keep[Q][256];
             for_each_feq<L, true>(rho, u, uu, ddf, [&](auto qc, float e, float fe0) {
                 constexpr int q = decltype(qc)::value;
                 const float ds = kbc_shear<L, q>(P);
                 const float dh = (f[q] - e) - ds;
+                dh_keep[q][threadIdx.x] = dh;
                 if (!(dh == 0.f && fe0 == fe0 && fe0 != 0.f)) {
                     sp1 += ds * dh / fe0;
                     sp2 += dh * dh / fe0;
@@ -352,11 +356,10 @@ __device__ __forceinline__ void collide(float (&f)[L::Q], float tau, const StepA
             const float g_num = (2.f - inv_beta) * sp1, g_den = sp2 + 1e-32f;
             const float g_q = (g_num == 0.f && g_den > 0.f && g_den < __int_as_float(0x7f800000)) ? g_num : g_num / g_den;
             const float gamma = inv_beta - g_q;
-            for_each_feq<L>(rho, u, uu, ddf, [&](auto qc, float e) {
-                constexpr int q = decltype(qc)::value;
+            static_for<0, Q>([&](auto qc) {
+                constexpr int q = qc.value;
                 const float ds = kbc_shear<L, q>(P);
-                const float dh = (f[q] - e) - ds;
-                f[q] -= beta * (2.f * ds + gamma * dh);
+                f[q] -= beta * (2.f * ds + gamma * dh_keep[q][threadIdx.x]);
             });
         }
     }
