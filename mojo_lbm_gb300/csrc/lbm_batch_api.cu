@@ -37,6 +37,7 @@ struct lbm_batch {
     uint8_t* d_box_sum = nullptr;
     uint8_t* d_tile_near = nullptr;
     uint8_t* d_flags_seen = nullptr;  // the flags of the last summary, 256 cells per unit
+    uint2* d_cell_masks = nullptr;    // neighbour-solid masks per cell, 256 cells per unit
     uint32_t* d_changed = nullptr;    // summary round in which a box summary last changed
     uint32_t summary_gen = 0;
     bool summary_valid = false;
@@ -82,6 +83,18 @@ __global__ void batch_near_kernel(const BatchArgs b, const uint8_t* box_sum, uin
     if (*changed != gen) return;  // the same value for every thread
     const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
     write_near_mask(i, b.total_units * kTileWarps, batch_near_box(b, i, box_sum), tile_near);
+}
+
+// The neighbour-solid masks of the cells of every warp with its mask bit set, one block per unit,
+// after a change of the flags in this round (*changed == gen).
+template <class L>
+__global__ void __launch_bounds__(256) batch_cell_mask_kernel(const BatchArgs b, const uint32_t* changed,
+                                                              uint32_t gen) {
+    if (*changed != gen) return;  // the same value for every thread
+    const uint32_t u = blockIdx.x;
+    const uint32_t d = find_domain(b.unit_begin, b.ndom, u);
+    const StepArgs& a = b.dom[d];
+    tile_cell_masks<L>(a, u - b.unit_begin[d], const_cast<uint2*>(a.cell_masks));
 }
 
 // The summary byte of every warp box of the batch whose flags changed; one thread per box.
@@ -175,6 +188,7 @@ lbm_status lbm_batch_create(const lbm_config_t* cfg, int32_t n_domains, const lb
     if (e == cudaSuccess) e = cudaMalloc(&b->d_box_sum, units > 0 ? units * kTileWarps : 1);
     if (e == cudaSuccess) e = cudaMalloc(&b->d_tile_near, units > 0 ? units : 1);
     if (e == cudaSuccess) e = cudaMalloc(&b->d_flags_seen, units > 0 ? units * kTileCells : 1);
+    if (e == cudaSuccess) e = cudaMalloc(&b->d_cell_masks, sizeof(uint2) * (units > 0 ? units * kTileCells : 1));
     if (e == cudaSuccess) e = cudaMalloc(&b->d_changed, sizeof(uint32_t));
     if (e == cudaSuccess) e = cudaMemset(b->d_changed, 0, sizeof(uint32_t));
     if (e == cudaSuccess)
@@ -197,6 +211,7 @@ lbm_status lbm_batch_destroy(lbm_batch* b) {
     cudaFree(b->d_box_sum);
     cudaFree(b->d_tile_near);
     cudaFree(b->d_flags_seen);
+    cudaFree(b->d_cell_masks);
     cudaFree(b->d_changed);
     if (b->capture_stream) cudaStreamDestroy(b->capture_stream);
     delete b;
@@ -237,6 +252,7 @@ lbm_status lbm_batch_set_domain(lbm_batch* b, int32_t i, void* f_a, void* f_b, f
     a.cap_rho = b->cfg.capture_density;
     a.cap_u = b->cfg.capture_velocity;
     a.tile_near = b->d_tile_near + b->unit_begin[i];
+    a.cell_masks = b->d_cell_masks + (size_t)b->unit_begin[i] * kTileCells;
     a.mx = (uint32_t)g.tx - 1u;
     a.my = (uint32_t)g.ty - 1u;
     a.shx = (uint32_t)ilog2(g.tx);
@@ -308,6 +324,15 @@ lbm_status lbm_batch_run(lbm_batch* b, int64_t n_steps, int64_t first_step, void
         if (nboxes)
             batch_near_kernel<<<(nboxes + 255u) / 256u, 256, 0, s>>>(a, b->d_box_sum, b->d_tile_near, b->d_changed,
                                                                     b->summary_gen);
+        LBM_BCK(cudaGetLastError());
+        if (nboxes) {
+            if (b->lattice == LBM_D2Q9)
+                batch_cell_mask_kernel<D2Q9><<<a.total_units, kTileCells, 0, s>>>(a, b->d_changed, b->summary_gen);
+            else if (b->lattice == LBM_D3Q19)
+                batch_cell_mask_kernel<D3Q19><<<a.total_units, kTileCells, 0, s>>>(a, b->d_changed, b->summary_gen);
+            else
+                batch_cell_mask_kernel<D3Q27><<<a.total_units, kTileCells, 0, s>>>(a, b->d_changed, b->summary_gen);
+        }
         LBM_BCK(cudaGetLastError());
     }
     const int64_t chunk = 64;

@@ -51,6 +51,15 @@ __global__ void __launch_bounds__(256) tile_near_kernel(const uint8_t* __restric
     write_near_mask(i, nboxes, bit, tile_near);
 }
 
+// The neighbour-solid masks of every cell in a warp with its mask bit set (one block per tile),
+// after a change of the flags in this round (*changed == gen).
+template <class L>
+__global__ void __launch_bounds__(256) cell_mask_kernel(const StepArgs a, uint2* __restrict__ masks,
+                                                        const uint32_t* changed, uint32_t gen) {
+    if (*changed != gen) return;  // the same value for every thread
+    tile_cell_masks<L>(a, blockIdx.x, masks);
+}
+
 thread_local std::string g_err;
 
 lbm_status fail(lbm_status s, const std::string& msg) {
@@ -87,6 +96,7 @@ struct lbm_handle {
     StepLaunch step_learned;  // block-per-tile kernel with the learned closure (LES handles), or null
     int path;              // 0 auto, 1 generic only, 2 block-per-tile only
     uint8_t* box_sum;      // per warp box (32 cells): summary byte (flags other than 0 inside, on faces)
+    uint2* cell_masks;     // per cell: neighbour-solid masks, written for the warps with a mask bit set
     uint8_t* flags_seen;   // the flags the summary was built from
     uint32_t* changed;     // device word: summary round in which a box summary last changed
     uint32_t summary_gen;  // summary rounds issued
@@ -143,6 +153,7 @@ StepArgs step_args(const lbm_handle* h, const void* f_in, void* f_out, float* bc
     a.closure = h->closure_on ? h->closure : nullptr;
     a.cl = h->closure_uniform;
     a.tile_near = h->tile_near;
+    a.cell_masks = h->cell_masks;
     a.mx = h->mx;
     a.my = h->my;
     a.shx = h->shx;
@@ -171,6 +182,13 @@ lbm_status tile_summary(lbm_handle* h, const uint8_t* flags, cudaStream_t s) {
     h->summary_valid = 1;
     tile_near_kernel<<<(nboxes + 255u) / 256u, 256, 0, s>>>(h->box_sum, h->lay, nboxes, h->tile_near, h->changed,
                                                              gen);
+    LBM_CK(cudaGetLastError());
+    const StepArgs a = step_args(h, nullptr, nullptr, nullptr, flags, 1.f, 0);
+    switch (h->grid.lattice) {
+        case LBM_D2Q9: cell_mask_kernel<D2Q9><<<h->ntiles, kTileCells, 0, s>>>(a, h->cell_masks, h->changed, gen); break;
+        case LBM_D3Q19: cell_mask_kernel<D3Q19><<<h->ntiles, kTileCells, 0, s>>>(a, h->cell_masks, h->changed, gen); break;
+        default: cell_mask_kernel<D3Q27><<<h->ntiles, kTileCells, 0, s>>>(a, h->cell_masks, h->changed, gen); break;
+    }
     LBM_CK(cudaGetLastError());
     return LBM_OK;
 }
@@ -300,6 +318,7 @@ lbm_status lbm_create(const lbm_config_t* cfg, const lbm_grid_t* grid, lbm_handl
     h->shx = (uint32_t)ilog2(grid->tx);
     h->shxy = (uint32_t)(ilog2(grid->tx) + ilog2(grid->ty));
     h->box_sum = nullptr;
+    h->cell_masks = nullptr;
     h->flags_seen = nullptr;
     h->changed = nullptr;
     h->summary_gen = 0;
@@ -317,6 +336,7 @@ lbm_status lbm_create(const lbm_config_t* cfg, const lbm_grid_t* grid, lbm_handl
     if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&h->capture_stream, cudaStreamNonBlocking);
     if (e == cudaSuccess && h->step_tile) e = cudaMalloc(&h->box_sum, (size_t)h->ntiles * kTileWarps);
     if (e == cudaSuccess && h->step_tile) e = cudaMalloc(&h->flags_seen, (size_t)h->lay.ncells);
+    if (e == cudaSuccess && h->step_tile) e = cudaMalloc(&h->cell_masks, sizeof(uint2) * (size_t)h->lay.ncells);
     if (e == cudaSuccess && h->step_tile) e = cudaMalloc(&h->changed, sizeof(uint32_t));
     if (e == cudaSuccess && h->step_tile) e = cudaMemset(h->changed, 0, sizeof(uint32_t));
     if (e == cudaSuccess && h->step_tile) e = cudaMalloc(&h->tile_near, h->ntiles);
@@ -334,6 +354,7 @@ lbm_status lbm_destroy(lbm_handle* h) {
     if (h->scratch) cudaFree(h->scratch);
     if (h->box_sum) cudaFree(h->box_sum);
     if (h->flags_seen) cudaFree(h->flags_seen);
+    if (h->cell_masks) cudaFree(h->cell_masks);
     if (h->changed) cudaFree(h->changed);
     if (h->tile_near) cudaFree(h->tile_near);
     if (h->closure) cudaFree(h->closure);

@@ -36,6 +36,7 @@ struct StepArgs {
     ClosureUniform cl;         // and its warp-uniform part
     const uint8_t* tile_near;  // per tile: bit w set if a cell of warp w or a cell it pulls from
                                // holds a flag other than plain FLUID (warp_near)
+    const uint2* cell_masks;   // per cell of such a warp: (raw_solid, nib_solid), cell_solid_masks
     uint32_t mx, my, shx, shxy; // lx = t & mx, ly = (t >> shx) & my, lz = t >> shxy
 };
 
@@ -767,6 +768,41 @@ __device__ __forceinline__ void write_near_mask(uint32_t i, uint32_t nboxes, uin
     if (i < nboxes && (lane & 7u) == 0u) tile_near[i / kTileWarps] = (uint8_t)(m >> lane);
 }
 
+// set_adjacent_flags (ops/load_and_store.mojo:270-291) for the cell at flag offset n with cell
+// deltas dc: bit q of raw_solid when the flag at x - c_q is SOLID (the raw compare of the
+// mid-grid bounce-back, ops/load_and_store.mojo:216), of nib_solid when its enum nibble is SOLID
+// (the moving wall, ops/boundary_condition.mojo:77).
+template <class L>
+__device__ __forceinline__ uint2 cell_solid_masks(const uint8_t* __restrict__ flags, uint32_t n,
+                                                  const int32_t (&dc)[3][3]) {
+    uint32_t raw_solid = 0u, nib_solid = 0u;
+    static_for<1, L::Q>([&](auto qc) {
+        constexpr int q = qc.value;
+        constexpr int sx = -L::c(q, 0), sy = -L::c(q, 1), sz = -L::c(q, 2);
+        const uint8_t pf = __ldg(flags + ((int32_t)n + dc[0][sx + 1] + dc[1][sy + 1] + dc[2][sz + 1]));
+        if (pf == LBM_FLAG_SOLID) raw_solid |= 1u << q;
+        if ((pf & 0x0F) == LBM_FLAG_SOLID) nib_solid |= 1u << q;
+    });
+    return make_uint2(raw_solid, nib_solid);
+}
+
+// The masks of every cell of the tile's warps whose mask bit is set, for the step to load instead
+// of gathering its neighbours' flags (the block of 256 threads of tile `tile`).
+template <class L>
+__device__ __forceinline__ void tile_cell_masks(const StepArgs& a, uint32_t tile, uint2* __restrict__ masks) {
+    const uint32_t tid = threadIdx.x;
+    if (((__ldg(a.tile_near + tile) >> (tid >> 5)) & 1u) == 0u) return;  // warp-uniform
+    const uint32_t byz = a.lay.d_ntx.div(tile);
+    const uint32_t bx = tile - byz * (uint32_t)a.lay.ntx;
+    const uint32_t bz = a.lay.d_nty.div(byz);
+    const uint32_t by = byz - bz * (uint32_t)a.lay.nty;
+    const uint32_t lx = tid & a.mx, ly = (tid >> a.shx) & a.my, lz = tid >> a.shxy;
+    int32_t dc[3][3], dp[3][3];
+    tile_deltas<L::D>(a, bx, by, bz, lx, ly, lz, (int32_t)(kTileCells * L::Q), dc, dp);
+    const uint32_t n = tid + kTileCells * tile;
+    masks[n] = cell_solid_masks<L>(a.flags, n, dc);
+}
+
 // The per-thread body of the block-per-tile step: thread `tid` of the CTA that owns tile `tile`.
 // Every lane of a warp must call it (the learned closure `cl`, staged in shared memory, is
 // evaluated by whole warps).  Learned closure: fbuf is this warp's
@@ -840,16 +876,13 @@ __device__ __forceinline__ void tile_step(const StepArgs& a, const uint32_t tile
     }
 
     if (!clean) {
-        // ---- neighbour flags at x - c_q (set_adjacent_flags, ops/load_and_store.mojo:270-291)
+        // ---- neighbour flags at x - c_q, as masks built when the flags last changed
+        // (cell_solid_masks: set_adjacent_flags, ops/load_and_store.mojo:270-291)
         uint32_t raw_solid = 0u, nib_solid = 0u;
         if (!ESO || a.moving) {
-            static_for<1, Q>([&](auto qc) {
-                constexpr int q = qc.value;
-                constexpr int sx = -L::c(q, 0), sy = -L::c(q, 1), sz = -L::c(q, 2);
-                const uint8_t pf = __ldg(a.flags + ((int32_t)n + dc[0][sx + 1] + dc[1][sy + 1] + dc[2][sz + 1]));
-                if (pf == LBM_FLAG_SOLID) raw_solid |= 1u << q;
-                if ((pf & 0x0F) == LBM_FLAG_SOLID) nib_solid |= 1u << q;
-            });
+            const uint2 m = __ldg(a.cell_masks + n);
+            raw_solid = m.x;
+            nib_solid = m.y;
         }
         if constexpr (!ESO) {
             // mid-grid bounce-back on a raw SOLID compare (ops/load_and_store.mojo:216)
