@@ -1,10 +1,10 @@
 """Decaying Taylor–Green vortex in a periodic box: the flow the learned closure is trained and
-judged on.
+evaluated on.
 
 A fine D3Q19 run is box-filtered onto the grid of half its resolution; the filtered fields give
 the closure's training pairs (strain invariants -> the eddy viscosity that best explains the
 subgrid stress) and the reference against which coarse LES runs (Smagorinsky, learned) are
-judged by kinetic energy and energy spectrum.  Conventions: the box is [0, 2 pi)^3 with N cells
+measured by kinetic energy and energy spectrum.  Conventions: the box is [0, 2 pi)^3 with N cells
 per side, L = N / (2 pi) cells, u0 the lattice velocity amplitude, Re = u0 L / nu, one
 convective time unit L / u0 steps.  The initial field is the analytic vortex
 u = u0 sin x cos y cos z, v = -u0 cos x sin y cos z, w = 0 plus a seeded divergence-free

@@ -194,7 +194,7 @@ def test_closure_rejections():
 
 
 def test_trained_closure_beats_smagorinsky_on_small_tgv():
-    """Train on a box-filtered 128^3 Taylor-Green run (seed 1), judge 64^3 LES runs against the
+    """Train on a box-filtered 128^3 Taylor-Green run (seed 1), evaluate 64^3 LES runs against the
     filtered 128^3 run of seed 0 by their energy spectra."""
     from mojo_lbm_gb300 import tgv
     res = tgv.study(N_fine=128, Re=400.0, train_times=(2, 3, 4, 5, 6), eval_times=(3, 5, 7), train_steps=400,
