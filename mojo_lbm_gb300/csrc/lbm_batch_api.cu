@@ -1,6 +1,8 @@
 // C ABI of the batched persistent step (lbm_batch_* in include/lbm_gb300.h).
 #include <cuda_runtime.h>
 
+#include <algorithm>
+
 #include <cstring>
 #include <map>
 #include <string>
@@ -91,10 +93,11 @@ template <class L>
 __global__ void __launch_bounds__(256) batch_cell_mask_kernel(const BatchArgs b, const uint32_t* changed,
                                                               uint32_t gen) {
     if (*changed != gen) return;  // the same value for every thread
-    const uint32_t u = blockIdx.x;
-    const uint32_t d = find_domain(b.unit_begin, b.ndom, u);
-    const StepArgs& a = b.dom[d];
-    tile_cell_masks<L>(a, u - b.unit_begin[d], const_cast<uint2*>(a.cell_masks));
+    for (uint32_t u = blockIdx.x; u < b.total_units; u += gridDim.x) {  // blocks stride over the units
+        const uint32_t d = find_domain(b.unit_begin, b.ndom, u);
+        const StepArgs& a = b.dom[d];
+        tile_cell_masks<L>(a, u - b.unit_begin[d], const_cast<uint2*>(a.cell_masks));
+    }
 }
 
 // The summary byte of every warp box of the batch whose flags changed; one thread per box.
@@ -326,12 +329,13 @@ lbm_status lbm_batch_run(lbm_batch* b, int64_t n_steps, int64_t first_step, void
                                                                     b->summary_gen);
         LBM_BCK(cudaGetLastError());
         if (nboxes) {
+            const uint32_t grid = std::min<uint32_t>(a.total_units, (uint32_t)b->sms * 8u);
             if (b->lattice == LBM_D2Q9)
-                batch_cell_mask_kernel<D2Q9><<<a.total_units, kTileCells, 0, s>>>(a, b->d_changed, b->summary_gen);
+                batch_cell_mask_kernel<D2Q9><<<grid, kTileCells, 0, s>>>(a, b->d_changed, b->summary_gen);
             else if (b->lattice == LBM_D3Q19)
-                batch_cell_mask_kernel<D3Q19><<<a.total_units, kTileCells, 0, s>>>(a, b->d_changed, b->summary_gen);
+                batch_cell_mask_kernel<D3Q19><<<grid, kTileCells, 0, s>>>(a, b->d_changed, b->summary_gen);
             else
-                batch_cell_mask_kernel<D3Q27><<<a.total_units, kTileCells, 0, s>>>(a, b->d_changed, b->summary_gen);
+                batch_cell_mask_kernel<D3Q27><<<grid, kTileCells, 0, s>>>(a, b->d_changed, b->summary_gen);
         }
         LBM_BCK(cudaGetLastError());
     }

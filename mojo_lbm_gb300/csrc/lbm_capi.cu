@@ -2,6 +2,7 @@
 // the per-lattice kernel tables, the graph-replayed time loop, and the auxiliary kernels.
 #include <cuda_runtime.h>
 
+#include <algorithm>
 #include <cmath>
 #include <cstdio>
 #include <cstring>
@@ -51,13 +52,14 @@ __global__ void __launch_bounds__(256) tile_near_kernel(const uint8_t* __restric
     write_near_mask(i, nboxes, bit, tile_near);
 }
 
-// The neighbour-solid masks of every cell in a warp with its mask bit set (one block per tile),
-// after a change of the flags in this round (*changed == gen).
+// The neighbour-solid masks of every cell in a warp with its mask bit set (256 threads per tile,
+// blocks striding over the tiles: a launch with nothing to do is one short wave), after a change of
+// the flags in this round (*changed == gen).
 template <class L>
 __global__ void __launch_bounds__(256) cell_mask_kernel(const StepArgs a, uint2* __restrict__ masks,
-                                                        const uint32_t* changed, uint32_t gen) {
+                                                        const uint32_t* changed, uint32_t gen, uint32_t ntiles) {
     if (*changed != gen) return;  // the same value for every thread
-    tile_cell_masks<L>(a, blockIdx.x, masks);
+    for (uint32_t tile = blockIdx.x; tile < ntiles; tile += gridDim.x) tile_cell_masks<L>(a, tile, masks);
 }
 
 thread_local std::string g_err;
@@ -184,10 +186,11 @@ lbm_status tile_summary(lbm_handle* h, const uint8_t* flags, cudaStream_t s) {
                                                              gen);
     LBM_CK(cudaGetLastError());
     const StepArgs a = step_args(h, nullptr, nullptr, nullptr, flags, 1.f, 0);
+    const uint32_t grid = std::min<uint32_t>(h->ntiles, (uint32_t)h->sm_count * 8u);
     switch (h->grid.lattice) {
-        case LBM_D2Q9: cell_mask_kernel<D2Q9><<<h->ntiles, kTileCells, 0, s>>>(a, h->cell_masks, h->changed, gen); break;
-        case LBM_D3Q19: cell_mask_kernel<D3Q19><<<h->ntiles, kTileCells, 0, s>>>(a, h->cell_masks, h->changed, gen); break;
-        default: cell_mask_kernel<D3Q27><<<h->ntiles, kTileCells, 0, s>>>(a, h->cell_masks, h->changed, gen); break;
+        case LBM_D2Q9: cell_mask_kernel<D2Q9><<<grid, kTileCells, 0, s>>>(a, h->cell_masks, h->changed, gen, h->ntiles); break;
+        case LBM_D3Q19: cell_mask_kernel<D3Q19><<<grid, kTileCells, 0, s>>>(a, h->cell_masks, h->changed, gen, h->ntiles); break;
+        default: cell_mask_kernel<D3Q27><<<grid, kTileCells, 0, s>>>(a, h->cell_masks, h->changed, gen, h->ntiles); break;
     }
     LBM_CK(cudaGetLastError());
     return LBM_OK;
