@@ -140,19 +140,6 @@ __device__ __forceinline__ void closure_features(const float* S, float s2, float
 }
 
 
-// Next layer's A fragments from a layer's accumulators: the accumulator layout of m16n8k16 (rows
-// g, g+8; columns 2t, 2t+1) is the A layout of the next k-slice, n-tiles 2kc and 2kc+1 forming
-// k-slice kc.  ReLU and BF16 rounding in one instruction per pair.
-__device__ __forceinline__ void relu_to_a(const float (&h)[4][4], uint32_t (&a)[2][4]) {
-#pragma unroll
-    for (int kc = 0; kc < 2; ++kc) {
-        a[kc][0] = relu_bf16x2(h[2 * kc][0], h[2 * kc][1]);
-        a[kc][1] = relu_bf16x2(h[2 * kc][2], h[2 * kc][3]);
-        a[kc][2] = relu_bf16x2(h[2 * kc + 1][0], h[2 * kc + 1][1]);
-        a[kc][3] = relu_bf16x2(h[2 * kc + 1][2], h[2 * kc + 1][3]);
-    }
-}
-
 // nu_t of the calling lane's cell; every lane of the warp must call it.  c: the per-lane
 // fragments in shared memory; u: the uniform part; stage: 32 x uint4 of per-warp shared memory,
 // ys: 32 floats of per-warp shared memory.  in_range reports whether the normalised features
