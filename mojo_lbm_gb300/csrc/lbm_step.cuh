@@ -933,9 +933,13 @@ __device__ __forceinline__ void tile_step(const StepArgs& a, const uint32_t tile
 #ifndef LBM_TILE_MIN_BLOCKS
 #define LBM_TILE_MIN_BLOCKS 5
 #endif
+// resident CTAs per SM the KBC and D3Q27 kernels are built for (their register demand is higher)
+#ifndef LBM_TILE_MIN_BLOCKS_HEAVY
+#define LBM_TILE_MIN_BLOCKS_HEAVY 3
+#endif
 
 template <class L, int METHOD, bool F16C, int COLL, int LES>
-__global__ void __launch_bounds__(256, (L::Q == 9) ? 5 : ((COLL == LBM_KBC || L::Q == 27) ? 3 : LBM_TILE_MIN_BLOCKS))
+__global__ void __launch_bounds__(256, (L::Q == 9) ? 5 : ((COLL == LBM_KBC || L::Q == 27) ? LBM_TILE_MIN_BLOCKS_HEAVY : LBM_TILE_MIN_BLOCKS))
     step_kernel_tile(const StepArgs a) {
     static_assert(LES != kLesLearned, "the learned closure runs in step_kernel_learned");
     tile_step<L, METHOD, F16C, COLL, LES>(a, blockIdx.x, threadIdx.x);
