@@ -83,6 +83,47 @@ def test_batch_equals_single_domain_steps(variant):
         assert torch.equal(got_b, fb), f"domain {i} lattice B differs"
 
 
+def test_batch_full_size_equals_single_domain_steps():
+    """The batched benchmark configuration at its full size: 512 channels (61 M cells, sizes on a
+    32-cell granule, 32 x 8 tiles, Bouzidi links on every cylinder), one 64-step graph replay and
+    two direct steps, against each channel stepped alone."""
+    from mojo_lbm_gb300.workloads import channel_specs, cylinder_channels
+    chans = cylinder_channels(tile=(32, 8, 1), specs=channel_specs(512, 0, granule=(32, 32)))
+    assert sum(c.grid.num_points for c in chans) > 60_000_000
+    cfg = chans[0].cfg
+    steps = 66
+    batch = BatchSolver([c.grid for c in chans], cfg)
+    gen = torch.Generator(device="cuda").manual_seed(7)
+    solvers, bufs, ref = [], [], []
+    for i, ch in enumerate(chans):
+        s = Solver(ch.grid, cfg)
+        fa = torch.empty(ch.grid.num_points * 9, device="cuda")
+        u = torch.empty((2,) + ch.grid.shape, device="cuda").uniform_(-0.02, 0.02, generator=gen)
+        s.init_equilibrium(fa, 1.0, ch.tau, u)
+        fb = fa.clone()
+        bc = torch.from_numpy(ch.bc).cuda()
+        fl = torch.from_numpy(ch.flags).cuda()
+        batch.set_domain(i, fa, fb, bc, fl, ch.tau)
+        solvers.append(s)
+        bufs.append((fa, fb, bc, fl))
+        ref.append((fa.clone(), fb.clone()))
+    batch.set_links(*links_of(chans), 0.0)
+    batch.run(steps, 0)
+    for i, ch in enumerate(chans):
+        s, (fa, fb), (_, _, bc, fl) = solvers[i], ref[i], bufs[i]
+        ids = torch.from_numpy(ch.body.fluid_boundaries_list).cuda()
+        dirs = torch.from_numpy(ch.body.lattice_links_list).cuda()
+        dists = torch.from_numpy(ch.body.link_distances_list).cuda()
+        for k in range(steps):
+            src, dst = (fa, fb) if k % 2 == 0 else (fb, fa)
+            s.double_buffer_step(dst, src, bc, fl, ch.tau)
+            s.linkwise_bounceback(dst, None, ids, dirs, dists, Bounceback_method.BOUZIDI, False, 0.0)
+    torch.cuda.synchronize()
+    for i in range(len(chans)):
+        assert torch.equal(bufs[i][0], ref[i][0]), f"domain {i} lattice A differs"
+        assert torch.equal(bufs[i][1], ref[i][1]), f"domain {i} lattice B differs"
+
+
 def test_batch_rejects_unsupported_tiles():
     from mojo_lbm_gb300 import LBM_Grid, get_D2Q9
     with pytest.raises(Exception, match="256-cell"):
