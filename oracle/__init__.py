@@ -1,9 +1,10 @@
 """TEST INFRASTRUCTURE — ctypes wrapper of the CPU oracle (liblbm_oracle.so).
 
 Only tests/, __graft_entry__.smoke() and bench.py's CPU-baseline leg import this module, as
-the checker or as the timed CPU reference; the product never does.  Parity with the reference
+the values the tests compare against or as the timed CPU baseline; the product never does.  Parity with the reference
 is UNPINNED (see lbm_oracle.cpp): the reference is Mojo and its repository has no golden
-vectors for the step; the oracle is pinned to the Ghia et al. cavity fixture and invariants.
+vectors for the step; the oracle is pinned to the Ghia et al. cavity fixture, the DFG drag the
+reference recorded, and invariants.
 """
 from __future__ import annotations
 

@@ -1,4 +1,4 @@
-"""TEST INFRASTRUCTURE — float64 numpy restatement of the learned closure's network, the checker
+"""TEST INFRASTRUCTURE — float64 numpy restatement of the learned closure's network, the oracle
 of the CUDA training kernels (lbm_mlp_forward / lbm_mlp_backward / lbm_mlp_adam).
 
 Only tests/ import this module.  The network is 8 -> 32 -> 32 -> 1 with ReLU hidden layers and

@@ -2,7 +2,7 @@
  * TEST INFRASTRUCTURE — CPU oracle for the fused LBM stream–collide step.
  *
  * Only the tests, __graft_entry__.smoke() and bench.py's CPU-baseline leg load this library,
- * and only as the checker or the timed CPU reference.  The product (mojo_lbm_gb300, the CUDA
+ * and only as the values the tests compare against or as the timed CPU baseline.  The product (mojo_lbm_gb300, the CUDA
  * library) never calls it.
  *
  * It restates, scalar and cell by cell, the algorithm of JohnCSu/mojo_lbm's GPU step in the
@@ -12,9 +12,11 @@
  *
  * PARITY UNPINNED: the reference is Mojo 1.0 / MAX 26.5, which is not installed here, and its
  * repository holds no golden vectors for this path (its tests are compile-and-run scripts,
- * compiletest.py:21-80).  The oracle is checked against the only fixture the reference holds for
- * the path — the Ghia et al. lid-driven-cavity centre lines (benchmarks/LDC/) — and against
- * conservation and symmetry invariants.
+ * compiletest.py:21-80).  The oracle is checked against the fixtures the reference holds for the
+ * path — the Ghia et al. lid-driven-cavity centre lines (benchmarks/LDC/) and the DFG Re = 20
+ * cylinder drag the reference recorded at three resolutions
+ * (benchmarks/Cylinder2D/CylinderFlow_Re20.mojo) — and against conservation and symmetry
+ * invariants.
  *
  * Deviations from the reference, each deliberate:
  *  - capture_density/capture_velocity store rho into bc[x,y,z,D] and u into bc[x,y,z,0..D-1];

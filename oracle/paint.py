@@ -1,4 +1,4 @@
-"""Test infrastructure: numpy restatement of the reference's wall and shape painting, the checker
+"""Test infrastructure: numpy restatement of the reference's wall and shape painting, the oracle
 of the library's device painting (lbm_paint_*).  Not part of the product.
 
 Arrays are flat host arrays in the grid's tiled layout (flags uint8, bc float32 with D+1

@@ -1,4 +1,4 @@
-"""Host-side checks of the learned closure: the float64 numpy network (the checker of the CUDA
+"""Host-side checks of the learned closure: the float64 numpy network (the oracle of the CUDA
 training kernels) against central finite differences, the C++ oracle's closure (BF16 emulation)
 against the numpy network, the feature definitions of the oracle against the package's training
 features, the packing of lbm_closure_t, and the Smagorinsky fallback of the oracle's LES step."""
