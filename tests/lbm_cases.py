@@ -7,7 +7,7 @@ import math
 import numpy as np
 
 import oracle
-from mojo_lbm_gb300 import Flags, LBM_Config, LBM_Grid, preprocess
+from mojo_lbm_gb300 import Flags, LBM_Config, LBM_Grid, LBM_method, preprocess
 from mojo_lbm_gb300.lattice import get_lattice as get_lattice_by_id
 
 LATTICES = {"D2Q9": 0, "D3Q19": 1, "D3Q27": 2}
@@ -109,3 +109,26 @@ def fluid_mask_pop(grid: LBM_Grid, flags: np.ndarray) -> np.ndarray:
     for q in range(grid.Q):
         m[loc + lay.T * (q + grid.Q * tile)] = keep
     return m
+
+
+def step_case(lat: str, meth: str, store: str, coll: str, les: bool, case: str, shape, tile):
+    """A seeded step case, the recipe of the step-parity tests: 'mixed' (random flags over every
+    boundary branch, capture bits, EXCLUDE, free NaN bc components) or 'ldc' (closed cavity with a
+    moving lid).  Returns (grid, cfg, flags, bc, f0, tau)."""
+    import zlib
+
+    grid = make_grid(lat, shape, tile)
+    f16 = store == "f16c"
+    method = LBM_method.DOUBLE_BUFFER if meth == "db" else LBM_method.ESOTERIC_PULL
+    seed = zlib.crc32(f"{lat}/{meth}/{store}/{coll}/{les}/{case}".encode())
+    rng = np.random.default_rng(seed)
+    if case == "mixed":
+        cfg = LBM_Config(method, collision_op=coll, LES=les, BCs={Flags.EQUILIBRIUM}, DDF_shift=f16 or bool(seed % 2),
+                         use_float16c=f16, capture_density=True, capture_velocity=True)
+        flags, bc = mixed_flags(grid, rng)
+    else:
+        cfg = LBM_Config(method, collision_op=coll, LES=les, DDF_shift=f16, use_float16c=f16)
+        flags, bc = ldc_flags(grid, cfg, 0.1)
+    tau = 0.55 if coll == "KBC" else 0.8
+    f0 = initial_f(grid, cfg, rng, tau=tau)
+    return grid, cfg, flags, bc, f0, tau

@@ -244,3 +244,26 @@ def test_dfg_fixture():
         mod = importlib.util.module_from_spec(spec)
         spec.loader.exec_module(mod)
         assert mod.extract(src.read_text()) == fix
+
+
+# ---- the oracle's own goldens (tests/golden/oracle_goldens.json) --------------------------------
+def test_oracle_goldens():
+    """The float32 oracle reproduces the committed SHA-256 digests of its output (f after 6 steps and
+    the bc array) on the 192 seeded step cases; the digests of the inputs are checked first, so a
+    change of the case recipe (or of numpy's generator) is told apart from a change of the oracle."""
+    import importlib.util
+    spec = importlib.util.spec_from_file_location("make_oracle_goldens", GOLDEN / "make_oracle_goldens.py")
+    mod = importlib.util.module_from_spec(spec)
+    spec.loader.exec_module(mod)
+    fix = json.loads((GOLDEN / "oracle_goldens.json").read_text())
+    assert fix["steps"] == mod.STEPS and len(fix["cases"]) == len(mod.CASES) == 192
+    changed_in, changed_out = [], []
+    for c in mod.CASES:
+        d_in, d_out = mod.run_case(c)
+        want = fix["cases"][mod.case_id(c)]
+        if d_in != want["inputs"]:
+            changed_in.append(mod.case_id(c))
+        elif d_out != want["outputs"]:
+            changed_out.append(mod.case_id(c))
+    assert not changed_in, f"inputs of {len(changed_in)} cases differ from the fixture's: {changed_in[:4]}"
+    assert not changed_out, f"oracle output of {len(changed_out)} cases changed: {changed_out[:4]}"
