@@ -21,7 +21,7 @@ import torch
 import oracle
 from mojo_lbm_gb300 import Flags, LBM_Config, LBM_method
 from mojo_lbm_gb300.solver import Solver
-from tests.lbm_cases import initial_f, ldc_flags, make_grid, mixed_flags
+from tests.lbm_cases import initial_f, ldc_flags, make_grid, mixed_flags, step_case
 
 pytestmark = pytest.mark.gpu
 
@@ -96,20 +96,8 @@ CASES = list(itertools.product(["D2Q9", "D3Q19", "D3Q27"], ["db", "eso"], ["fp32
                          ids=["-".join(map(str, c)) for c in CASES])
 def test_step_parity(lat, meth, store, coll, les, case, kernel):
     shape, tile = (SHAPES if kernel == "generic" else TILE_SHAPES)[lat]
-    grid = make_grid(lat, shape, tile)
-    f16 = store == "f16c"
-    method = LBM_method.DOUBLE_BUFFER if meth == "db" else LBM_method.ESOTERIC_PULL
-    seed = zlib.crc32(f"{lat}/{meth}/{store}/{coll}/{les}/{case}".encode())
-    rng = np.random.default_rng(seed)
-    if case == "mixed":
-        cfg = LBM_Config(method, collision_op=coll, LES=les, BCs={Flags.EQUILIBRIUM}, DDF_shift=f16 or bool(seed % 2),
-                         use_float16c=f16, capture_density=True, capture_velocity=True)
-        flags, bc = mixed_flags(grid, rng)
-    else:
-        cfg = LBM_Config(method, collision_op=coll, LES=les, DDF_shift=f16, use_float16c=f16)
-        flags, bc = ldc_flags(grid, cfg, 0.1)
-    tau = 0.55 if coll == "KBC" else 0.8
-    f0 = initial_f(grid, cfg, rng, tau=tau)
+    # the recipe of the oracle's goldens (tests/golden/make_oracle_goldens.py)
+    grid, cfg, flags, bc, f0, tau = step_case(lat, meth, store, coll, les, case, shape, tile)
     got, ref, bc_gpu, bc_ref = run_both(grid, cfg, flags, bc, f0, tau, STEPS, path=1 if kernel == "generic" else 2)
     assert_close(got, ref, cfg, f"{lat}/{meth}/{store}/{coll}/LES={les}/{case}/{kernel}")
     if case == "mixed":
