@@ -8,7 +8,6 @@ pin both.  Regenerate after a deliberate change to the oracle or to the case rec
 """
 from __future__ import annotations
 
-import hashlib
 import itertools
 import json
 import sys
@@ -21,20 +20,13 @@ import numpy as np  # noqa: E402
 
 import oracle  # noqa: E402
 from mojo_lbm_gb300 import LBM_method  # noqa: E402
-from tests.lbm_cases import step_case  # noqa: E402
+from tests.lbm_cases import digest, step_case  # noqa: E402
 
 OUT = Path(__file__).with_name("oracle_goldens.json")
 STEPS = 6
 SHAPES = {"D2Q9": ((30, 20, 1), (10, 5, 1)), "D3Q19": ((18, 12, 10), (6, 4, 5)), "D3Q27": ((12, 12, 10), (4, 6, 5))}
 CASES = list(itertools.product(["D2Q9", "D3Q19", "D3Q27"], ["db", "eso"], ["fp32", "f16c"],
                                ["SRT", "TRT", "KBC", "RLBM"], [False, True], ["mixed", "ldc"]))
-
-
-def digest(*arrays) -> str:
-    h = hashlib.sha256()
-    for a in arrays:
-        h.update(np.ascontiguousarray(a).tobytes())
-    return h.hexdigest()
 
 
 def case_id(c) -> str:

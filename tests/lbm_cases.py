@@ -132,3 +132,13 @@ def step_case(lat: str, meth: str, store: str, coll: str, les: bool, case: str, 
     tau = 0.55 if coll == "KBC" else 0.8
     f0 = initial_f(grid, cfg, rng, tau=tau)
     return grid, cfg, flags, bc, f0, tau
+
+
+def digest(*arrays) -> str:
+    """SHA-256 of the arrays' bytes, in order (the oracle goldens' digests)."""
+    import hashlib
+
+    h = hashlib.sha256()
+    for a in arrays:
+        h.update(np.ascontiguousarray(a).tobytes())
+    return h.hexdigest()

@@ -12,7 +12,9 @@ all auxiliary outputs are compared bit for bit.
 from __future__ import annotations
 
 import itertools
+import json
 import zlib
+from pathlib import Path
 
 import numpy as np
 import pytest
@@ -21,11 +23,12 @@ import torch
 import oracle
 from mojo_lbm_gb300 import Flags, LBM_Config, LBM_method
 from mojo_lbm_gb300.solver import Solver
-from tests.lbm_cases import initial_f, ldc_flags, make_grid, mixed_flags, step_case
+from tests.lbm_cases import digest, initial_f, ldc_flags, make_grid, mixed_flags, step_case
 
 pytestmark = pytest.mark.gpu
 
 STEPS = 6
+GOLDENS = json.loads((Path(__file__).with_name("golden") / "oracle_goldens.json").read_text())
 # generic kernel: non-power-of-two tiles; block-per-tile kernel: 256-cell power-of-two tiles
 SHAPES = {"D2Q9": ((30, 20, 1), (10, 5, 1)), "D3Q19": ((18, 12, 10), (6, 4, 5)), "D3Q27": ((12, 12, 10), (4, 6, 5))}
 TILE_SHAPES = {"D2Q9": ((32, 32, 1), (16, 16, 1)), "D3Q19": ((16, 16, 8), (8, 8, 4)), "D3Q27": ((16, 8, 16), (4, 8, 8))}
@@ -103,6 +106,11 @@ def test_step_parity(lat, meth, store, coll, les, case, kernel):
     if case == "mixed":
         # captured rho/u written into bc
         assert np.array_equal(bc_gpu.view(np.uint32), bc_ref.view(np.uint32))
+    if kernel == "generic":
+        # the committed digest of this case's output (tests/golden/oracle_goldens.json)
+        assert GOLDENS["steps"] == STEPS and GOLDENS["shapes"][lat] == [list(shape), list(tile)]
+        want = GOLDENS["cases"]["-".join(map(str, (lat, meth, store, coll, les, case)))]["outputs"]
+        assert digest(got, bc_gpu) == want
 
 
 @pytest.mark.parametrize("lat", ["D2Q9", "D3Q19", "D3Q27"])
