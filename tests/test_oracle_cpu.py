@@ -267,3 +267,29 @@ def test_oracle_goldens():
             changed_out.append(mod.case_id(c))
     assert not changed_in, f"inputs of {len(changed_in)} cases differ from the fixture's: {changed_in[:4]}"
     assert not changed_out, f"oracle output of {len(changed_out)} cases changed: {changed_out[:4]}"
+
+
+# ---- the reference's velocity sets (tests/golden/lattices.json) ---------------------------------
+@pytest.mark.parametrize("lid,name,pylat", [(0, "D2Q9", get_D2Q9), (1, "D3Q19", get_D3Q19), (2, "D3Q27", get_D3Q27)])
+def test_lattices_match_reference_fixture(lid, name, pylat):
+    """The oracle's and the package's velocity sets are the reference's: the directions in its order
+    and the weights equal to its fractions as float32 (the reference's float_dtype); where the
+    reference is present, extracting it again gives the same fixture."""
+    import importlib.util
+    import os
+    fix = json.loads((GOLDEN / "lattices.json").read_text())
+    ref = fix[name]
+    c, w, o = oracle.lattice(lid)
+    L = pylat()
+    dirs = np.array(ref["directions"])
+    assert dirs.shape == (L.Q, L.D)
+    assert np.array_equal(c[:, : L.D], dirs) and np.array_equal(L.directions, dirs)
+    wref = np.array([a / b for a, b in ref["weights"]], np.float64).astype(np.float32)
+    assert np.array_equal(w.astype(np.float32), wref) and np.array_equal(L.weights.astype(np.float32), wref)
+    assert all(np.array_equal(dirs[q], -dirs[q + 1]) and o[q] == q + 1 for q in range(1, L.Q, 2))
+    src = Path(os.environ.get("REF", "/root/reference")) / fix["source"]
+    if src.exists():
+        spec = importlib.util.spec_from_file_location("make_lattice_fixture", GOLDEN / "make_lattice_fixture.py")
+        mod = importlib.util.module_from_spec(spec)
+        spec.loader.exec_module(mod)
+        assert mod.extract(src.read_text()) == fix
