@@ -161,3 +161,36 @@ def test_sphere_link_parameter():
     assert q == pytest.approx(0.5)
     q = get_q_for_sphere(np.array([1.0, 1.0, 0]), np.array([0.0, 0.0, 0]), c, 1.0)
     assert 0 <= q <= 1 and q == pytest.approx(1 - 1 / math.sqrt(2))
+
+
+def test_flags_and_config_defaults_match_reference_fixture():
+    """The node flags (package, C header) and LBM_Config's keyword defaults (package and
+    lbm_config_default) are the reference's, as extracted into tests/golden/constants.json; where
+    the reference is present, extracting it again gives the same fixture."""
+    import importlib.util
+    import json
+    import os
+    golden = Path(__file__).with_name("golden")
+    fix = json.loads((golden / "constants.json").read_text())
+    header = HEADER.read_text()
+    assert len(fix["flags"]) == 7
+    for name, value in fix["flags"].items():
+        assert getattr(Flags, name) == value, name
+        m = re.search(rf"LBM_FLAG_{name}\s*=\s*(0x[0-9a-fA-F]+|\d+)", header)
+        assert m and int(m.group(1), 0) == value, name
+    d = fix["config_defaults"]
+    py = LBM_Config()
+    c = _capi.lbm_config_t()
+    assert _capi.lib().lbm_config_default(C.byref(c), 0) == 0
+    for k in ("LES", "DDF_shift", "use_float16c", "include_moving_boundary", "capture_density", "capture_velocity"):
+        assert getattr(py, k) == d[k] and bool(getattr(c, k)) == d[k], k
+    assert py.collision_op == d["collision_op"] == "SRT" and c.collision_op == 0
+    # BCs = {} is the reference's default, to which it always adds FLUID and SOLID
+    assert d["BCs"] == [] and py.INCLUDED_BCs == {Flags.FLUID, Flags.SOLID} and c.include_equilibrium_bc == 0
+    assert d["f_dtype"] is None and py.f_dtype is None
+    ref = Path(os.environ.get("REF", "/root/reference"))
+    if (ref / fix["flags_source"]).exists() and (ref / fix["config_source"]).exists():
+        spec = importlib.util.spec_from_file_location("make_constants_fixture", golden / "make_constants_fixture.py")
+        mod = importlib.util.module_from_spec(spec)
+        spec.loader.exec_module(mod)
+        assert mod.extract((ref / fix["flags_source"]).read_text(), (ref / fix["config_source"]).read_text()) == fix
