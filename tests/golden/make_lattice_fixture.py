@@ -1,7 +1,8 @@
 """Extracts the reference's velocity sets from src/lbm/lattice.mojo (get_D2Q9, get_D3Q19, get_D3Q27):
 the directions in the reference's order (rest first, each direction followed by its opposite) and
-the weights as the numerator / denominator pairs the reference writes, into lattices.json.  Run in
-a checkout that has the reference at REF (default /root/reference)."""
+the weights as the numerator / denominator pairs the reference writes, and the order of the
+symmetric stress components (get_stress_indices) for D = 2 and 3, into lattices.json.  Run in a
+checkout that has the reference at REF (default /root/reference)."""
 import json
 import os
 import re
@@ -39,6 +40,14 @@ def extract(text: str) -> dict:
             if m:
                 weights.append([float(m.group(1)), float(m.group(2))])
         out[name] = {"directions": dirs, "weights": weights}
+    i = text.index("def get_stress_indices[")
+    nxt = text.find("\ndef ", i + 1)
+    body = text[i: nxt if nxt >= 0 else len(text)]
+    out["stress_pairs"] = {}
+    for d in (2, 3):
+        j = body.index(f"elif D == {d}:")
+        k = body.index("return", j)
+        out["stress_pairs"][str(d)] = [[int(a), int(b)] for a, b in re.findall(r"\[\s*(\d)\s*,\s*(\d)\s*\]", body[j:k])]
     return out
 
 

@@ -272,9 +272,9 @@ def test_oracle_goldens():
 # ---- the reference's velocity sets (tests/golden/lattices.json) ---------------------------------
 @pytest.mark.parametrize("lid,name,pylat", [(0, "D2Q9", get_D2Q9), (1, "D3Q19", get_D3Q19), (2, "D3Q27", get_D3Q27)])
 def test_lattices_match_reference_fixture(lid, name, pylat):
-    """The oracle's and the package's velocity sets are the reference's: the directions in its order
-    and the weights equal to its fractions as float32 (the reference's float_dtype); where the
-    reference is present, extracting it again gives the same fixture."""
+    """The oracle's and the package's velocity sets are the reference's: the directions in its order,
+    the weights equal to its fractions as float32 (the reference's float_dtype) and the order of the
+    stress components; where the reference is present, extracting it again gives the same fixture."""
     import importlib.util
     import os
     fix = json.loads((GOLDEN / "lattices.json").read_text())
@@ -287,6 +287,7 @@ def test_lattices_match_reference_fixture(lid, name, pylat):
     wref = np.array([a / b for a, b in ref["weights"]], np.float64).astype(np.float32)
     assert np.array_equal(w.astype(np.float32), wref) and np.array_equal(L.weights.astype(np.float32), wref)
     assert all(np.array_equal(dirs[q], -dirs[q + 1]) and o[q] == q + 1 for q in range(1, L.Q, 2))
+    assert [list(p) for p in L.stress_indices] == fix["stress_pairs"][str(L.D)]
     src = Path(os.environ.get("REF", "/root/reference")) / fix["source"]
     if src.exists():
         spec = importlib.util.spec_from_file_location("make_lattice_fixture", GOLDEN / "make_lattice_fixture.py")
