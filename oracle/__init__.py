@@ -44,6 +44,7 @@ def lib() -> C.CDLL:
         h.oracle_f16c_encode.argtypes = [vp, vp, i64]
         h.oracle_f16c_decode.argtypes = [vp, vp, i64]
         h.oracle_layout_offset.argtypes = [vp, i64, i64, i64, i64, i64]
+        h.oracle_stress_pairs.argtypes = [i32, vp]
         h.oracle_layout_offset.restype = i64
         h.oracle_lattice.argtypes = [i32, vp, vp, vp]
         h.oracle_max_threads.restype = i32
@@ -150,6 +151,13 @@ def f16c_decode(h: np.ndarray) -> np.ndarray:
 def layout_offset(grid, x, y, z, k, K) -> int:
     g = grid.to_c()
     return int(lib().oracle_layout_offset(C.byref(g), x, y, z, k, K))
+
+
+def stress_pairs(D: int) -> list[list[int]]:
+    """The (alpha, beta) pairs of the stress components, in the order the step sums them."""
+    out = np.zeros(12, dtype=np.int32)
+    n = lib().oracle_stress_pairs(int(D), _p(out))
+    return out[: 2 * n].reshape(n, 2).tolist()
 
 
 def lattice(lattice_id: int):

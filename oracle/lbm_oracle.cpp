@@ -1,9 +1,9 @@
 /*
  * TEST INFRASTRUCTURE — CPU oracle for the fused LBM stream–collide step.
  *
- * Only the tests, __graft_entry__.smoke() and bench.py's CPU-baseline leg load this library,
- * and only as the values the tests compare against or as the timed CPU baseline.  The product (mojo_lbm_gb300, the CUDA
- * library) never calls it.
+ * Only the tests, __graft_entry__.smoke() and bench.py's CPU-baseline leg load this library, and
+ * only as the values the tests compare against or as the timed CPU baseline.  The product
+ * (mojo_lbm_gb300, the CUDA library) never calls it.
  *
  * It restates, scalar and cell by cell, the algorithm of JohnCSu/mojo_lbm's GPU step in the
  * same operation order (sequential sums over q = 0..Q-1, src/utils/vector.mojo:205-224).  It is
@@ -15,8 +15,9 @@
  * compiletest.py:21-80).  The oracle is checked against the fixtures the reference holds for the
  * path — the Ghia et al. lid-driven-cavity centre lines (benchmarks/LDC/) and the DFG Re = 20
  * cylinder drag the reference recorded at three resolutions
- * (benchmarks/Cylinder2D/CylinderFlow_Re20.mojo) — and against conservation and symmetry
- * invariants.
+ * (benchmarks/Cylinder2D/CylinderFlow_Re20.mojo) — against the velocity sets, stress-component
+ * order, node flags and configuration defaults extracted from the reference's sources, and against
+ * conservation and symmetry invariants.
  *
  * Deviations from the reference, each deliberate:
  *  - capture_density/capture_velocity store rho into bc[x,y,z,D] and u into bc[x,y,z,0..D-1];
@@ -973,6 +974,15 @@ int oracle_lattice(int id, int32_t* c_out /* Q*3 */, double* w_out, int32_t* opp
         opp_out[q] = L.opp[q];
     }
     return L.Q;
+}
+
+/* The stress-component pairs (alpha, beta) the step uses for dimension D (2 or 3); returns their
+ * count (get_stress_indices, lattice.mojo:352-398). */
+int oracle_stress_pairs(int D, int32_t* out /* n*2 */) {
+    const int n = D == 2 ? 3 : 6;
+    for (int k = 0; k < n; ++k)
+        for (int j = 0; j < 2; ++j) out[2 * k + j] = D == 2 ? kStress2[k][j] : kStress3[k][j];
+    return n;
 }
 
 /* Learned closure for the LES steps that follow (copied; NULL returns to Smagorinsky). */
