@@ -107,7 +107,8 @@ lbm_status lbm_config_default(lbm_config_t* cfg, int32_t lbm_method);
 
 /* Host-only validation of a (config, grid) pair; needs no GPU.  The reference enforces the
  * same rules with comptime asserts (config.mojo:153, grid.mojo:301-305,345-365,434-438,
- * kernels/esoteric_pull.mojo:76-78). */
+ * kernels/esoteric_pull.mojo:76-78).  Also refused here: fewer than 1 or 2^32 or more cells
+ * (cell indices are 32-bit), a NaN Cs, and a negative Cs with LES. */
 lbm_status lbm_validate(const lbm_config_t* cfg, const lbm_grid_t* grid);
 
 /* Number of populations / spatial dimension of a lattice id, or -1. */

@@ -284,7 +284,7 @@ lbm_status lbm_validate(const lbm_config_t* c, const lbm_grid_t* g) {
         return fail(LBM_EINVAL, "Tile size must divide nx, ny and nz");
     const int64_t N = (int64_t)g->nx * g->ny * g->nz;
     if (N >= (int64_t)1 << 32) return fail(LBM_EINVAL, "grid has 2^32 or more cells");
-    if (c->use_float16c && !(c->Cs == c->Cs)) return fail(LBM_EINVAL, "Cs is NaN");
+    if (!(c->Cs == c->Cs)) return fail(LBM_EINVAL, "Cs is NaN");
     if (c->LES && !(c->Cs >= 0.0f)) return fail(LBM_EINVAL, "Cs must be non-negative");
     return LBM_OK;
 }

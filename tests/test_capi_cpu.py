@@ -81,6 +81,36 @@ def test_validate_rules():
     assert [lib.lbm_lattice_d(i) for i in range(4)] == [2, 3, 3, -1]
 
 
+def test_validate_edges():
+    """Smallest and largest grids, extents, and the Smagorinsky constant."""
+    lib = _capi.lib()
+    c = DoubleBufferConfig().to_c()
+
+    def check(grid, cfg=c):
+        return lib.lbm_validate(C.byref(cfg), C.byref(grid))
+
+    # the smallest grids of each dimension (check_model_match_dim counts extents above 1)
+    assert check(_capi.lbm_grid_t(0, 2, 2, 1, 1, 1, 1)) == 0
+    assert check(_capi.lbm_grid_t(1, 2, 2, 2, 2, 2, 2)) == 0
+    assert check(_capi.lbm_grid_t(1, 1, 1, 1, 1, 1, 1)) == _capi.LBM_EINVAL
+    assert b"dimension" in lib.lbm_last_error()
+    for g in (_capi.lbm_grid_t(1, 0, 16, 16, 8, 8, 4), _capi.lbm_grid_t(1, 16, -16, 16, 8, 8, 4)):
+        assert check(g) == _capi.LBM_EINVAL and b"positive" in lib.lbm_last_error()
+    assert check(_capi.lbm_grid_t(1, 16, 16, 16, 0, 8, 4)) == _capi.LBM_EINVAL
+    assert b"tile extents" in lib.lbm_last_error()
+    # cell indices are 32-bit: 2^32 cells are refused, one row fewer is accepted
+    assert check(_capi.lbm_grid_t(0, 65536, 65536, 1, 16, 16, 1)) == _capi.LBM_EINVAL
+    assert b"2^32" in lib.lbm_last_error()
+    assert check(_capi.lbm_grid_t(0, 65536, 65520, 1, 16, 16, 1)) == 0
+    # Cs: NaN is refused in every configuration, a negative value with LES
+    g = _capi.lbm_grid_t(1, 16, 16, 16, 8, 8, 4)
+    for les, cs, ok in ((False, float("nan"), False), (True, float("nan"), False), (True, -0.1, False),
+                        (False, -0.1, True), (True, 0.0, True)):
+        cc = DoubleBufferConfig(LES=les).to_c()
+        cc.Cs = cs
+        assert (check(g, cc) == 0) == ok, (les, cs)
+
+
 def test_handle_calls_reject_null():
     lib = _capi.lib()
     assert lib.lbm_double_buffer_step(None, None, None, None, None, 0.8, None) == _capi.LBM_EINVAL
