@@ -48,6 +48,11 @@ WORKLOADS = {
                                          Re=10000.0, U=0.1, tile=(8, 8, 4),
                                          desc="D3Q27 KBC + Smagorinsky Cs=0.1 lid-driven cube 256^3, Re=10000, "
                                               "Float16C + DDF shift, FP32 math, esoteric-pull in place"),
+    # the reference's CPU-runnable configuration (its 2D cavity examples, examples/LDC.mojo)
+    "ldc2d_d2q9_256_fp32": dict(lattice="D2Q9", n=256, method="db", coll="SRT", les=False, f16=False, Re=100.0,
+                                U=0.1, tile=(16, 16, 1), full_steps=20000,
+                                desc="D2Q9 SRT lid-driven cavity 256x256, FP32, Re=100, lid u=0.1, rest equilibrium "
+                                     "init, bounce-back walls + moving-wall lid, pull streaming (20k-step run)"),
     "batch2d_cylinders_512": dict(lattice="D2Q9", n=0, method="db", coll="SRT", les=False, f16=False, batch=512,
                                   tile=(16, 16, 1), autotune=True,
                                   desc="512 D2Q9 SRT cylinder channels, nx ~ U[200,800], ny = 0.41 nx (sizes on a 32-cell granule, tile autotuned), "
@@ -165,6 +170,36 @@ class ClockSampler:
                 "reasons": reasons, "samples": len(rows)}
 
 
+def timed_repeats(run_k, stream, dev, world: int, min_seconds: float, max_repeats: int = 100000):
+    """Times run_k() (K steps) between CUDA events on the launching stream, with a barrier and a
+    synchronize on both sides of every repeat, until min_seconds of timed work have passed (at
+    least one repeat).  Returns the per-repeat times in ms.  All ranks run the same number of
+    repeats (rank 0's count is broadcast after the first repeat)."""
+    import torch
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    times: list[float] = []
+    n_target = None
+    while True:
+        barrier(world)
+        torch.cuda.synchronize(dev)
+        e0.record(stream)
+        run_k()
+        e1.record(stream)
+        torch.cuda.synchronize(dev)
+        barrier(world)
+        times.append(e0.elapsed_time(e1))
+        if n_target is None:
+            n = max(1, min(max_repeats, math.ceil(min_seconds * 1e3 / max(times[0], 1e-3))))
+            if world > 1:
+                import torch.distributed as dist
+                t = torch.tensor([n], dtype=torch.int64, device=dev)
+                dist.broadcast(t, 0)
+                n = int(t.item())
+            n_target = n
+        if len(times) >= n_target:
+            return times
+
+
 # ---------------------------------------------------------------------------------------------
 def build_case(wl: dict):
     """Grid, config, host flags/bc and tau of a workload (host numpy, tiled layout)."""
@@ -172,26 +207,28 @@ def build_case(wl: dict):
     from mojo_lbm_gb300.lattice import get_lattice
     lat_id = {"D2Q9": 0, "D3Q19": 1, "D3Q27": 2}[wl["lattice"]]
     n = wl["n"]
-    grid = LBM_Grid(get_lattice(lat_id), n, n, n, wl["tile"])
+    grid = LBM_Grid(get_lattice(lat_id), n, n, 1 if lat_id == 0 else n, wl["tile"])
     method = LBM_method.DOUBLE_BUFFER if wl["method"] == "db" else LBM_method.ESOTERIC_PULL
     N, D = grid.num_points, grid.D
     flags = np.zeros(N, np.uint8)
     bc = np.zeros(N * (D + 1), np.float32)
+    ar = wl.get("arith", "exact")
     if wl.get("kind") == "tgv":  # periodic, all fluid; tau from Re = u0 L / nu with L = n / (2 pi)
-        cfg = LBM_Config(method, collision_op=wl["coll"], LES=True, include_moving_boundary=False)
+        cfg = LBM_Config(method, collision_op=wl["coll"], LES=True, include_moving_boundary=False, arithmetic=ar)
         return grid, cfg, flags, bc, 3.0 * wl["U"] * (n / (2 * math.pi)) / wl["Re"] + 0.5
     if wl.get("kind") == "rest":  # periodic, all fluid, rest equilibrium, fixed tau
         cfg = LBM_Config(method, collision_op=wl["coll"], LES=wl["les"], DDF_shift=wl["f16"], use_float16c=wl["f16"],
-                         include_moving_boundary=False)
+                         include_moving_boundary=False, arithmetic=ar)
         return grid, cfg, flags, bc, wl["tau"]
     if wl.get("periodic"):  # diagnostic: the workload's kernel on a periodic box, no walls
         cfg = LBM_Config(method, collision_op=wl["coll"], LES=wl["les"], DDF_shift=wl["f16"], use_float16c=wl["f16"],
-                         include_moving_boundary=False)
+                         include_moving_boundary=False, arithmetic=ar)
         return grid, cfg, flags, bc, 3.0 * wl["U"] * (n - 1) / wl["Re"] + 0.5
-    cfg = LBM_Config(method, collision_op=wl["coll"], LES=wl["les"], DDF_shift=wl["f16"], use_float16c=wl["f16"])
-    for s in ("-Y", "+X", "-X", "+Z", "-Z"):
+    cfg = LBM_Config(method, collision_op=wl["coll"], LES=wl["les"], DDF_shift=wl["f16"], use_float16c=wl["f16"],
+                     arithmetic=ar)
+    for s in ("-Y", "+X", "-X") + (("+Z", "-Z") if D == 3 else ()):
         preprocess.set_exterior_walls(grid, cfg, flags, bc, s, Flags.SOLID, [0.0] * D, 1.0)
-    preprocess.set_exterior_walls(grid, cfg, flags, bc, "+Y", Flags.SOLID, [wl["U"], 0.0, 0.0], 1.0)
+    preprocess.set_exterior_walls(grid, cfg, flags, bc, "+Y", Flags.SOLID, [wl["U"]] + [0.0] * (D - 1), 1.0)
     tau = 3.0 * wl["U"] * (n - 1) / wl["Re"] + 0.5
     return grid, cfg, flags, bc, tau
 
@@ -206,8 +243,8 @@ def oracle_closure(wl: dict):
 
 
 def cpu_sample(wl: dict, grid, cfg, flags, bc, tau, budget_s: float, max_steps: int | None = None):
-    """Times the float32 CPU oracle (OpenMP over all host threads) on slabs of the same workload.
-    Returns (MLUPs, cores, description)."""
+    """Times the float32 CPU oracle (OpenMP over all host threads) on slabs of the same workload
+    (whole-grid steps for grids of at most 2^20 cells).  Returns (MLUPs, cores, description)."""
     import oracle
     N, Q = grid.num_points, grid.Q
     f = np.zeros(N * Q, oracle.f_dtype(cfg, 32))
@@ -215,7 +252,7 @@ def cpu_sample(wl: dict, grid, cfg, flags, bc, tau, budget_s: float, max_steps: 
     oracle.set_closure(oracle_closure(wl))
     f2 = f.copy() if wl["method"] == "db" else f
     cores = oracle.max_threads()
-    slab = max(1, N // 16)
+    slab = N if N <= (1 << 20) else max(1, N // 16)
     done_cells, t_total, k = 0, 0.0, 0
     while (t_total < budget_s or k < 2) and (max_steps is None or k < max_steps):
         b = (k * slab) % N
@@ -225,7 +262,8 @@ def cpu_sample(wl: dict, grid, cfg, flags, bc, tau, budget_s: float, max_steps: 
         done_cells += min(N, b + slab) - b
         k += 1
     oracle.set_closure(None)
-    return done_cells / t_total / 1e6, cores, f"{k} slab-steps of {slab} cells (1/16 of the grid) each, {t_total:.1f} s"
+    part = "the whole grid" if slab == N else "1/16 of the grid"
+    return done_cells / t_total / 1e6, cores, f"{k} slab-steps of {slab} cells ({part}) each, {t_total:.1f} s"
 
 
 # ---------------------------------------------------------------------------------------------
@@ -288,19 +326,14 @@ def run_ours(args, wl: dict):
     torch.cuda.synchronize(dev)
     single_ms = ev[0].elapsed_time(ev[1]) / 8
 
-    # timed region: K steps from the graph, barrier + synchronize on both sides
+    # timed region: K steps from the graph, barrier + synchronize on both sides, repeated until
+    # --repeat-seconds have passed so the clock sampler sees the GPU under load
     clocks = ClockSampler(local) if rank == 0 else None
     K = args.steps
-    barrier(world)
-    torch.cuda.synchronize(dev)
-    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-    e0.record(stream)
-    solver.run(fa, fb, bct, flt, tau, K, 0, stream)
-    e1.record(stream)
-    torch.cuda.synchronize(dev)
-    barrier(world)
-    local_ms = e0.elapsed_time(e1)
+    reps = timed_repeats(lambda: solver.run(fa, fb, bct, flt, tau, K, 0, stream), stream, dev, world,
+                         args.repeat_seconds)
     clk = clocks.stop() if clocks else None
+    local_ms = statistics.median(reps)
     t_ms, units = aggregate(local_ms, float(N) * K, world, dev)
     mlups = units / (t_ms * 1e-3) / 1e6
 
@@ -355,12 +388,9 @@ def run_ours(args, wl: dict):
         fb.copy_(fa)
         smag.run(fa, fb, bct, flt, tau, 64, 0, stream)
         torch.cuda.synchronize(dev)
-        s0, s1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-        s0.record(stream)
-        smag.run(fa, fb, bct, flt, tau, K, 0, stream)
-        s1.record(stream)
-        torch.cuda.synchronize(dev)
-        smag_mlups = float(N) * K / (s0.elapsed_time(s1) * 1e-3) / 1e6
+        s_reps = timed_repeats(lambda: smag.run(fa, fb, bct, flt, tau, K, 0, stream), stream, dev, 1,
+                               args.repeat_seconds)
+        smag_mlups = float(N) * K / (statistics.median(s_reps) * 1e-3) / 1e6
         smag.close()
         m = closure.meta
         extra = {"smagorinsky_mlups": round(smag_mlups, 2), "time_ratio_vs_smagorinsky": round(smag_mlups / mlups, 4),
@@ -388,7 +418,11 @@ def run_ours(args, wl: dict):
         "config": {"workload": wl["desc"], "grid": [grid.nx, grid.ny, grid.nz], "tile": list(grid.tile_shape),
                    "tile_source": wl.get("tile_source", "default of the workload"),
                    "layout": "reference tiled layout (col-major tile, col-major tiler)", "tau": round(tau, 6),
-                   "timing": "CUDA events around a K-step graph replay on the launching stream",
+                   "arithmetic": cfg.arithmetic,
+                   "timing": f"CUDA events around each of {len(reps)} replays of the K-step graph on the launching "
+                             f"stream (at least {args.repeat_seconds:g} s in all); value from the median replay "
+                             f"(min {min(reps) / K:.5f}, max {max(reps) / K:.5f} ms/step)",
+                   "repeats": len(reps),
                    "l2": "no flush: the two lattices (2 x %.2f GB) exceed the 129 MB L2" % (N * Q * (2 if wl["f16"] else 4) / 1e9),
                    "parallelism": f"replicas x{world}" if world > 1 else "single GPU"},
         "roofline": {"bound": "hbm", "achieved": round(achieved, 1), "peak": peak, "unit": "GB/s",
@@ -403,7 +437,7 @@ def run_ours(args, wl: dict):
                 "d2h_bytes_per_step": int(d2h / K),
                 "note": "Solver.run from pinned host buffers: upload of f, bc, flags and download of f inside the "
                         f"timed region, amortised over the {K} steps (after one untimed pass of 64 steps)"},
-        "gpu_launches": K + 3,
+        "gpu_launches": K + 3,  # per timed K-step replay
         "clocks": clk,
     }
     line.update(extra)
@@ -482,16 +516,9 @@ def run_batch(args, wl: dict):
     torch.cuda.synchronize(dev)
     K = args.steps
     clocks = ClockSampler(local) if rank == 0 else None
-    barrier(world)
-    torch.cuda.synchronize(dev)
-    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-    e0.record(stream)
-    batch.run(K, 0, stream)
-    e1.record(stream)
-    torch.cuda.synchronize(dev)
-    barrier(world)
+    reps = timed_repeats(lambda: batch.run(K, 0, stream), stream, dev, world, args.repeat_seconds)
     clk = clocks.stop() if clocks else None
-    t_ms, units = aggregate(e0.elapsed_time(e1), float(N) * K, world, dev)
+    t_ms, units = aggregate(statistics.median(reps), float(N) * K, world, dev)
     mlups = units / (t_ms * 1e-3) / 1e6
     launch_ms = t_ms / K  # one persistent step launch + one link launch per step, averaged
 
@@ -533,6 +560,9 @@ def run_batch(args, wl: dict):
         "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded channels from rest)",
         "config": {"workload": wl["desc"], "domains": len(chans), "cells": N, "links": int(ids.numel()),
                    "tile": list(wl["tile"]), "tile_source": tile_source,
+                   "timing": f"CUDA events around each of {len(reps)} replays of the K-step graph on the launching "
+                             f"stream (at least {args.repeat_seconds:g} s in all); value from the median replay",
+                   "repeats": len(reps),
                    "l2": "no flush: 2 x %.2f GB of lattices exceed L2" % (N * 36 / 1e9)},
         "roofline": {"bound": "hbm", "achieved": round(achieved, 1), "peak": peak, "unit": "GB/s",
                      "frac": round(achieved / peak, 4), "traffic": traffic,
@@ -659,6 +689,11 @@ def main(argv=None):
     ap.add_argument("--tile", type=str, default="", help="tile shape tx,ty,tz of the layout (default per workload)")
     ap.add_argument("--n", type=int, default=0, help="cube edge override (profiling on a smaller case)")
     ap.add_argument("--cpu-seconds", type=float, default=12.0)
+    ap.add_argument("--arithmetic", choices=["exact", "fast"], default=None,
+                    help="the step's arithmetic: exact (the reference's operation order, bit-identical to the "
+                         "float32 oracle) or fast (FMA rearranged, held to a float32 tolerance); default per workload")
+    ap.add_argument("--repeat-seconds", type=float, default=2.0,
+                    help="replay the timed K steps until this much timed work has passed (median replay reported)")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--autotune", action="store_true",
                     help="choose the layout's tile with the library's autotuner before the run")
@@ -671,6 +706,8 @@ def main(argv=None):
     if args.warmup < 3:
         ap.error("--warmup must be at least 3")
     wl = dict(WORKLOADS[args.workload])
+    if args.arithmetic:
+        wl["arith"] = args.arithmetic
     if args.tile:
         wl["tile"] = tuple(int(v) for v in args.tile.split(","))
     if args.domains and wl.get("batch"):

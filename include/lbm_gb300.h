@@ -41,7 +41,8 @@ typedef enum lbm_status {
     LBM_EINVAL = 1,       /* invalid argument or configuration                               */
     LBM_ECUDA = 2,        /* a CUDA runtime call failed                                      */
     LBM_ENAN = 3,         /* a reduction found a non-finite value                            */
-    LBM_ETIMEOUT = 4,     /* a bounded device wait gave up                                   */
+    LBM_ETIMEOUT = 4,     /* reserved for a bounded device wait that gives up; no kernel of  */
+                          /* this library waits on another, so no entry point returns it     */
     LBM_ENOMEM = 5,       /* a handle-owned allocation failed                                */
     LBM_EUNSUPPORTED = 6  /* the combination is not built (e.g. IBB with esoteric pull)      */
 } lbm_status;
@@ -69,12 +70,24 @@ enum {
 /* Bounceback_method (src/lbm/constants.mojo:120-123) */
 enum { LBM_BB_MID_GRID = 0, LBM_BB_BOUZIDI = 1 };
 
+/* Arithmetic of the step (no counterpart in the reference, whose step has one float32 form).
+ * LBM_ARITH_EXACT: every float32 operation in the reference's order, bit-identical to the
+ *   float32 CPU restatement of the reference step (the default).
+ * LBM_ARITH_FAST: the same operators rearranged for fused multiply-add (moments from opposite
+ *   pairs, one equilibrium evaluation per pair, approximate reciprocals and square roots,
+ *   Float16C codes handled in a scaled form), held to a float32 tolerance of the exact step:
+ *   after one step every float32 population within 1e-6 of it (plus 2e-6 relative for KBC and
+ *   LES), every Float16C code within 1 unit in the last place.  Used by the block-per-tile and
+ *   batched kernels; a grid those kernels do not take runs the exact arithmetic. */
+enum { LBM_ARITH_EXACT = 0, LBM_ARITH_FAST = 1 };
+
 /*
  * lbm_config_t mirrors LBM_Config (src/lbm/config.mojo:50-153).  The reference fixes these at
  * compile time; here they select a template instantiation at lbm_create.
  *   include_equilibrium_bc  <=>  Flags.EQUILIBRIUM in config.INCLUDED_BCs (config.mojo:141-151)
  *   Cs          Smagorinsky constant; the reference hard-codes 0.1 (steps/collide.mojo:200)
  *   trt_lambda  TRT magic parameter; the reference hard-codes 3/16 (steps/collide.mojo:214)
+ *   arithmetic  LBM_ARITH_EXACT (default) or LBM_ARITH_FAST
  * Fill with lbm_config_default() before changing fields.
  */
 typedef struct lbm_config_t {
@@ -89,6 +102,7 @@ typedef struct lbm_config_t {
     int32_t capture_velocity;
     float Cs;
     float trt_lambda;
+    int32_t arithmetic;
 } lbm_config_t;
 
 /* lbm_grid_t mirrors LBM_Grid's comptime shape and tile (src/lbm/grid.mojo:55-107). */
@@ -108,7 +122,8 @@ lbm_status lbm_config_default(lbm_config_t* cfg, int32_t lbm_method);
 /* Host-only validation of a (config, grid) pair; needs no GPU.  The reference enforces the
  * same rules with comptime asserts (config.mojo:153, grid.mojo:301-305,345-365,434-438,
  * kernels/esoteric_pull.mojo:76-78).  Also refused here: fewer than 1 or 2^32 or more cells
- * (cell indices are 32-bit), a NaN Cs, and a negative Cs with LES. */
+ * (cell indices are 32-bit), a NaN or negative Cs with LES, and an arithmetic other than
+ * LBM_ARITH_EXACT or LBM_ARITH_FAST. */
 lbm_status lbm_validate(const lbm_config_t* cfg, const lbm_grid_t* grid);
 
 /* Number of populations / spatial dimension of a lattice id, or -1. */
@@ -133,7 +148,8 @@ lbm_status lbm_set_block_threads(lbm_handle* h, int32_t threads);
 /* Kernel choice (no counterpart in the reference, which compiles one kernel per layout):
  * 0 = automatic (default), 1 = the generic kernel (any tile), 2 = the block-per-tile kernel,
  * which needs 256-cell tiles with power-of-two sides and Q*N < 2^31 (LBM_EUNSUPPORTED
- * otherwise).  Both produce identical populations. */
+ * otherwise).  With LBM_ARITH_EXACT both produce identical populations; the generic kernel
+ * always computes the exact arithmetic. */
 lbm_status lbm_set_kernel_path(lbm_handle* h, int32_t path);
 
 /* The kernel lbm_*_step will use: 1 generic, 2 block-per-tile, -1 for a null handle. */
@@ -199,7 +215,9 @@ lbm_status lbm_reduce_mass_momentum(lbm_handle* h, const void* f, const uint8_t*
  * sits where cudaMalloc/cudaFree must not run): it needs no handle and allocates nothing.  Its
  * scratch is a fixed 1 MiB device array in the library, held by every GPU that loads it until the
  * process exits, so grids above 2^27 cells (512^3) are rejected with LBM_EINVAL.  The first call
- * on a device looks that array up (cudaGetSymbolAddress); make it before any stream capture.
+ * on a device looks that array up (cudaGetSymbolAddress); make it before any stream capture.  The
+ * address is kept for the life of the process: do not call this on a device after a
+ * cudaDeviceReset of that device.
  * Calls share the array: calls that overlap on the GPU (other streams, other threads) race.
  * Same arguments and results as lbm_reduce_mass_momentum, with (cfg, grid) in place of a handle;
  * synchronises the stream. */

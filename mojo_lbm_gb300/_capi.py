@@ -29,7 +29,7 @@ class lbm_config_t(C.Structure):
                 ("DDF_shift", C.c_int32), ("use_float16c", C.c_int32),
                 ("include_moving_boundary", C.c_int32), ("include_equilibrium_bc", C.c_int32),
                 ("capture_density", C.c_int32), ("capture_velocity", C.c_int32),
-                ("Cs", C.c_float), ("trt_lambda", C.c_float)]
+                ("Cs", C.c_float), ("trt_lambda", C.c_float), ("arithmetic", C.c_int32)]
 
 
 class lbm_grid_t(C.Structure):

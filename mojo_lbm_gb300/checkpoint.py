@@ -31,7 +31,8 @@ def _config_fields(config) -> dict:
             "include_moving_boundary": bool(config.include_moving_boundary),
             "BCs": sorted(int(b) for b in config.INCLUDED_BCs),
             "capture_density": bool(config.capture_density), "capture_velocity": bool(config.capture_velocity),
-            "Cs": float(config.Cs), "trt_lambda": float(config.trt_lambda)}
+            "Cs": float(config.Cs), "trt_lambda": float(config.trt_lambda),
+            "arithmetic": getattr(config, "arithmetic", "exact")}
 
 
 def save(path, grid, config, *, f, bc, flags, step: int, tau: float, f2=None, extra: dict | None = None) -> Path:

@@ -12,6 +12,8 @@ from . import _capi
 from .constants import Collisions, Flags, LBM_method
 
 _FLAG_SET = {Flags.FLUID, Flags.SOLID, Flags.EQUILIBRIUM}
+# LBM_ARITH_EXACT / LBM_ARITH_FAST of the C header
+ARITHMETIC = {"exact": 0, "fast": 1}
 
 
 class LBM_Config:
@@ -19,13 +21,20 @@ class LBM_Config:
 
     ``Cs`` and ``trt_lambda`` are fixed in the reference (0.1 at steps/collide.mojo:200 and
     3/16 at :214); here they are run-time fields with the same defaults.
+
+    ``arithmetic`` has no counterpart in the reference: ``"exact"`` (default) computes every
+    float32 operation in the reference's order, bit-identical to the float32 restatement of the
+    reference step; ``"fast"`` rearranges the same operators for fused multiply-add and
+    approximate reciprocals and is held to a float32 tolerance of the exact step (block-per-tile
+    and batched kernels; other grids run the exact arithmetic).
     """
 
     def __init__(self, lbm_method: int = LBM_method.DOUBLE_BUFFER, *, collision_op: str = "SRT",
                  LES: bool = False, BCs: set[int] | None = None, DDF_shift: bool = False,
                  use_float16c: bool = False, f_dtype: str | None = None,
                  include_moving_boundary: bool = True, capture_density: bool = False,
-                 capture_velocity: bool = False, Cs: float = 0.1, trt_lambda: float = 3.0 / 16.0):
+                 capture_velocity: bool = False, Cs: float = 0.1, trt_lambda: float = 3.0 / 16.0,
+                 arithmetic: str = "exact"):
         if lbm_method not in LBM_method.valid_set:
             raise ValueError("lbm_method not valid")
         self.lbm_method = lbm_method
@@ -54,8 +63,11 @@ class LBM_Config:
         self.trt_lambda = float(trt_lambda)
         if not self.collision_op_is_valid():
             raise ValueError(f"Invalid Collision Operator specified: {collision_op}")
-        if math.isnan(self.Cs):
+        if self.LES and math.isnan(self.Cs):
             raise ValueError("Cs is NaN")
+        if arithmetic not in ARITHMETIC:
+            raise ValueError(f"arithmetic must be one of {sorted(ARITHMETIC)}")
+        self.arithmetic = arithmetic
 
     def implies_f_noneq(self, *, force: bool = False) -> bool:
         return self.LES or self.collision_op in Collisions.that_need_fneq or force
@@ -85,13 +97,14 @@ class LBM_Config:
         c.capture_velocity = int(self.capture_velocity)
         c.Cs = self.Cs
         c.trt_lambda = self.trt_lambda
+        c.arithmetic = ARITHMETIC[self.arithmetic]
         return c
 
     def __repr__(self) -> str:
         m = "DOUBLE_BUFFER" if self.lbm_method == LBM_method.DOUBLE_BUFFER else "ESOTERIC_PULL"
         return (f"LBM_Config({m}, collision_op={self.collision_op!r}, LES={self.LES}, DDF_shift={self.DDF_shift}, "
                 f"use_float16c={self.use_float16c}, include_moving_boundary={self.include_moving_boundary}, "
-                f"BCs={sorted(self.INCLUDED_BCs)})")
+                f"BCs={sorted(self.INCLUDED_BCs)}, arithmetic={self.arithmetic!r})")
 
 
 def DoubleBufferConfig(**kw) -> LBM_Config:

@@ -20,6 +20,9 @@ StepLaunch get_step_d3q27(int, int, int, int);
 StepLaunch get_tile_step_d2q9(int, int, int, int);
 StepLaunch get_tile_step_d3q19(int, int, int, int);
 StepLaunch get_tile_step_d3q27(int, int, int, int);
+StepLaunch get_fast_tile_step_d2q9(int, int, int, int);
+StepLaunch get_fast_tile_step_d3q19(int, int, int, int);
+StepLaunch get_fast_tile_step_d3q27(int, int, int, int);
 StepLaunch get_learned_step_d2q9(int, int, int);
 StepLaunch get_learned_step_d3q19(int, int, int);
 StepLaunch get_learned_step_d3q27(int, int, int);
@@ -117,9 +120,10 @@ struct lbm_handle {
     std::map<GraphKey, cudaGraphExec_t> graphs;
 };
 
-namespace {
+namespace lbm {
 
-LayoutDesc make_layout(const lbm_grid_t& g) {
+// The layout descriptor of a grid (shared with the allocation-free reduction, lbm_noalloc.cu).
+__attribute__((visibility("hidden"))) LayoutDesc make_layout(const lbm_grid_t& g) {
     LayoutDesc l;
     l.nx = g.nx; l.ny = g.ny; l.nz = g.nz;
     l.tx = g.tx; l.ty = g.ty; l.tz = g.tz;
@@ -133,6 +137,10 @@ LayoutDesc make_layout(const lbm_grid_t& g) {
     l.d_nty = FastDiv((uint32_t)l.nty);
     return l;
 }
+
+}  // namespace lbm
+
+namespace {
 
 StepArgs step_args(const lbm_handle* h, const void* f_in, void* f_out, float* bc, const uint8_t* flags, float tau,
                    int even) {
@@ -284,8 +292,10 @@ lbm_status lbm_validate(const lbm_config_t* c, const lbm_grid_t* g) {
         return fail(LBM_EINVAL, "Tile size must divide nx, ny and nz");
     const int64_t N = (int64_t)g->nx * g->ny * g->nz;
     if (N >= (int64_t)1 << 32) return fail(LBM_EINVAL, "grid has 2^32 or more cells");
-    if (!(c->Cs == c->Cs)) return fail(LBM_EINVAL, "Cs is NaN");
+    if (c->LES && !(c->Cs == c->Cs)) return fail(LBM_EINVAL, "Cs is NaN");
     if (c->LES && !(c->Cs >= 0.0f)) return fail(LBM_EINVAL, "Cs must be non-negative");
+    if (c->arithmetic != LBM_ARITH_EXACT && c->arithmetic != LBM_ARITH_FAST)
+        return fail(LBM_EINVAL, "arithmetic must be LBM_ARITH_EXACT or LBM_ARITH_FAST");
     return LBM_OK;
 }
 
@@ -306,7 +316,11 @@ lbm_status lbm_create(const lbm_config_t* cfg, const lbm_grid_t* grid, lbm_handl
     const int64_t Q = lattice_q(grid->lattice);
     const bool tile_ok = (int64_t)grid->tx * grid->ty * grid->tz == (int64_t)kTileCells && pow2(grid->tx) &&
                          pow2(grid->ty) && pow2(grid->tz) && Q * h->lay.ncells < ((int64_t)1 << 31);
+    const bool fast = cfg->arithmetic == LBM_ARITH_FAST;
     h->step_tile = !tile_ok ? nullptr
+                 : fast ? (grid->lattice == LBM_D2Q9 ? get_fast_tile_step_d2q9(m, f16, co, les)
+                           : grid->lattice == LBM_D3Q19 ? get_fast_tile_step_d3q19(m, f16, co, les)
+                                                        : get_fast_tile_step_d3q27(m, f16, co, les))
                  : grid->lattice == LBM_D2Q9 ? get_tile_step_d2q9(m, f16, co, les)
                  : grid->lattice == LBM_D3Q19 ? get_tile_step_d3q19(m, f16, co, les)
                                               : get_tile_step_d3q27(m, f16, co, les);

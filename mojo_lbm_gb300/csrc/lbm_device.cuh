@@ -187,6 +187,23 @@ LBM_HD uint32_t f16c_encode(float x) {
     return ((b >> 16) & 0x8000u) | mag;
 }
 
+// The scaled Float16C codec of the fast-arithmetic build (lbm_fast.cuh).
+// decode: the population times 2^-112, exact for every code (the code's magnitude bits placed at
+// float32 bits 12..26, its sign at bit 31: f16c_decode_sx without its multiplication).
+// encode: the code of xs * 2^112 from xs, rounded as the reference rounds (add 0x800 to the
+// float32 bits and drop 12 bits: the scaled float32 has the code's exponent field in place),
+// |xs| clamped first to the largest value of code 0x7FFF (infinities and NaN saturate: minNum
+// passes over a NaN).  Equal to f16c_encode(xs * 2^112) wherever xs is a normal float32; below
+// 2^-126 (populations below 2^-14) xs has already been rounded to a float32 denormal, 2^-149,
+// which is 2^-12 of a code's last place.
+LBM_HD float f16c_decode_scaled_sx(int32_t hs) { return as_f32(((uint32_t)hs << 12) & 0x87FFFFFFu); }
+
+LBM_HD uint32_t f16c_encode_scaled(float xs) {
+    constexpr float kSatScaled = 0x1.ffdp-112f;  // 1.999267578125 * 2^-112
+    const float m = fminf(fabsf(xs), kSatScaled);
+    return ((as_u32(xs) >> 16) & 0x8000u) | round_shift12(as_u32(m));
+}
+
 // ---------------------------------------------------------------------------------------------
 // Fast unsigned division by a runtime constant (Granlund & Montgomery, PLDI 1994; the
 // "round-up" variant valid for every 32-bit numerator).

@@ -48,6 +48,10 @@ template <> struct Pop<false> {
     static __device__ __forceinline__ float ld(const float* p) { return __ldg(p); }
     static __device__ __forceinline__ float ld_rw(const float* p) { return *p; }
     static __device__ __forceinline__ void st(float* p, float v) { *p = v; }
+    // float32 storage has no scaled form (the fast build scales Float16C codes only)
+    static __device__ __forceinline__ float ld_scaled(const float* p) { return __ldg(p); }
+    static __device__ __forceinline__ float ld_rw_scaled(const float* p) { return *p; }
+    static __device__ __forceinline__ void st_scaled(float* p, float v) { *p = v; }
 };
 template <> struct Pop<true> {
     using T = uint16_t;
@@ -59,6 +63,14 @@ template <> struct Pop<true> {
         return f16c_decode_sx(*reinterpret_cast<const int16_t*>(p));
     }
     static __device__ __forceinline__ void st(uint16_t* p, float v) { *p = (uint16_t)f16c_encode(v); }
+    // the fast build's scaled codes: population * 2^-112 (lbm_fast.cuh)
+    static __device__ __forceinline__ float ld_scaled(const uint16_t* p) {
+        return f16c_decode_scaled_sx(__ldg(reinterpret_cast<const int16_t*>(p)));
+    }
+    static __device__ __forceinline__ float ld_rw_scaled(const uint16_t* p) {
+        return f16c_decode_scaled_sx(*reinterpret_cast<const int16_t*>(p));
+    }
+    static __device__ __forceinline__ void st_scaled(uint16_t* p, float v) { *p = (uint16_t)f16c_encode_scaled(v); }
 };
 
 // Neighbour offsets along one axis for shifts -1, 0, +1 with the periodic wrap of
@@ -392,10 +404,17 @@ __device__ __forceinline__ void collide(float (&f)[L::Q], float tau, const StepA
     }
 }
 
+}  // namespace lbm
+
+#include "lbm_fast.cuh"
+
+namespace lbm {
+
 // moving_wall_bc (src/lbm/kernels/ops/boundary_condition.mojo:17-83): for pulls from a SOLID
 // (enum) node, f_q += 6 w_q rho_w (c_q . u_w) with u_w, rho_w read at the solid node.
-// bc_base(q) returns the element offset of component 0 of the pull neighbour's bc.
-template <class L, class BcBase>
+// bc_base(q) returns the element offset of component 0 of the pull neighbour's bc.  SCALED: f holds
+// populations times 2^-112 (the fast build's scaled Float16C codes), and so does the added term.
+template <class L, bool SCALED = false, class BcBase>
 __device__ __forceinline__ void moving_wall(float (&f)[L::Q], uint32_t nib_solid, const float* bc, uint32_t T,
                                             BcBase&& bc_base) {
     constexpr int Q = L::Q, D = L::D;
@@ -410,7 +429,8 @@ __device__ __forceinline__ void moving_wall(float (&f)[L::Q], uint32_t nib_solid
                 else if constexpr (L::c(q, d) < 0) cu -= bc[b + (uint64_t)T * d];
             });
             constexpr float six_w = 6.f * wf<L>(q);
-            f[q] += six_w * bc[b + (uint64_t)T * D] * cu;
+            if constexpr (SCALED) f[q] = __fmaf_rn((six_w * 0x1p-112f) * bc[b + (uint64_t)T * D], cu, f[q]);
+            else f[q] += six_w * bc[b + (uint64_t)T * D] * cu;
         }
     });
 }
@@ -807,7 +827,9 @@ __device__ __forceinline__ void tile_cell_masks(const StepArgs& a, uint32_t tile
 // Every lane of a warp must call it (the learned closure `cl`, staged in shared memory, is
 // evaluated by whole warps).  Learned closure: fbuf is this warp's
 // population stash ((Q+3)/4 x 32 float4 of shared memory).
-template <class L, int METHOD, bool F16C, int COLL, int LES>
+// FAST: the fast-arithmetic collision (collide_fast, lbm_fast.cuh), with scaled Float16C codes
+// when the collision is linear in f.
+template <class L, int METHOD, bool F16C, int COLL, int LES, bool FAST = false>
 __device__ __forceinline__ void tile_step(const StepArgs& a, const uint32_t tile, const uint32_t tid,
                                           const ClosureDev* cl = nullptr, float4* fbuf = nullptr,
                                           int32_t near = -1) {
@@ -816,6 +838,20 @@ __device__ __forceinline__ void tile_step(const StepArgs& a, const uint32_t tile
     constexpr int Q = L::Q, D = L::D, K = D + 1;
     constexpr uint32_t T = kTileCells;
     constexpr bool ESO = METHOD == LBM_ESOTERIC_PULL;
+    static_assert(!(FAST && LES == kLesLearned), "the learned closure has its own tolerance build");
+    constexpr bool SCALED = FAST && F16C && !LES && COLL != LBM_KBC;
+    auto ld = [](const S* p) -> float {
+        if constexpr (SCALED) return P::ld_scaled(p);
+        else return P::ld(p);
+    };
+    auto ld_rw = [](const S* p) -> float {
+        if constexpr (SCALED) return P::ld_rw_scaled(p);
+        else return P::ld_rw(p);
+    };
+    auto st = [](S* p, float v) {
+        if constexpr (SCALED) P::st_scaled(p, v);
+        else P::st(p, v);
+    };
 
     const uint32_t n = tid + T * tile;  // cell index = flag offset
     const uint32_t byz = a.lay.d_ntx.div(tile);
@@ -857,7 +893,7 @@ __device__ __forceinline__ void tile_step(const StepArgs& a, const uint32_t tile
             constexpr int q = qc.value;
             constexpr int sx = -L::c(q, 0), sy = -L::c(q, 1), sz = -L::c(q, 2);
             const int32_t o = own + dp[0][sx + 1] + dp[1][sy + 1] + dp[2][sz + 1];
-            f[q] = P::ld(fin + o + (int32_t)(T * q));
+            f[q] = ld(fin + o + (int32_t)(T * q));
         });
     } else {
         // even: pos from (x, pos), neg from (x + c_pos, neg); odd: pos from (x, neg), neg from
@@ -865,13 +901,13 @@ __device__ __forceinline__ void tile_step(const StepArgs& a, const uint32_t tile
         const bool ev = a.even != 0;
         const S* finA = fin + (ev ? 0u : T);
         const S* finB = fin + (ev ? T : 0u);
-        f[0] = P::ld_rw(fin + own);
+        f[0] = ld_rw(fin + own);
         static_for<1, Q - 1, 2>([&](auto qc) {
             constexpr int pos = qc.value, neg = pos + 1;
             constexpr int sx = L::c(pos, 0), sy = L::c(pos, 1), sz = L::c(pos, 2);
             const int32_t o = own + dp[0][sx + 1] + dp[1][sy + 1] + dp[2][sz + 1];
-            f[pos] = P::ld_rw(finA + own + (int32_t)(T * pos));
-            f[neg] = P::ld_rw(finB + o + (int32_t)(T * pos));
+            f[pos] = ld_rw(finA + own + (int32_t)(T * pos));
+            f[neg] = ld_rw(finB + o + (int32_t)(T * pos));
         });
     }
 
@@ -889,11 +925,11 @@ __device__ __forceinline__ void tile_step(const StepArgs& a, const uint32_t tile
             if (raw_solid)
                 static_for<1, Q>([&](auto qc) {
                     constexpr int q = qc.value;
-                    if ((raw_solid >> q) & 1u) f[q] = P::ld(fin + own + (int32_t)(T * opp<L>(q)));
+                    if ((raw_solid >> q) & 1u) f[q] = ld(fin + own + (int32_t)(T * opp<L>(q)));
                 });
         }
         if (a.moving && nib_solid) {
-            moving_wall<L>(f, nib_solid, a.bc, T, [&](auto qc) -> uint64_t {
+            moving_wall<L, SCALED>(f, nib_solid, a.bc, T, [&](auto qc) -> uint64_t {
                 constexpr int q = decltype(qc)::value;
                 constexpr int sx = -L::c(q, 0), sy = -L::c(q, 1), sz = -L::c(q, 2);
                 const uint32_t m = (uint32_t)((int32_t)n + dc[0][sx + 1] + dc[1][sy + 1] + dc[2][sz + 1]);
@@ -901,12 +937,16 @@ __device__ __forceinline__ void tile_step(const StepArgs& a, const uint32_t tile
                 return (uint64_t)(m - mt * T) + (uint64_t)T * K * mt;
             });
         }
-        if (a.eqbc && (flag & 0x0F) == LBM_FLAG_EQUILIBRIUM)
+        if (a.eqbc && (flag & 0x0F) == LBM_FLAG_EQUILIBRIUM) {
+            if constexpr (SCALED) static_for<0, Q>([&](auto qc) { f[qc.value] *= 0x1p112f; });
             equilibrium_bc<L>(f, a.bc, tid + (uint64_t)T * K * tile, T, (int32_t)(bx * tx + lx),
                               (int32_t)(by * ty + ly), (int32_t)(bz * tz + lz), a.lay, a.ddf != 0);
+            if constexpr (SCALED) static_for<0, Q>([&](auto qc) { f[qc.value] *= 0x1p-112f; });
+        }
     }
 
-    collide<L, COLL, LES>(f, a.tau, a, a.bc + (tid + (uint64_t)T * K * tile), T, flag, active, cl, fbuf);
+    if constexpr (FAST) collide_fast<L, COLL, LES, SCALED>(f, a, a.bc + (tid + (uint64_t)T * K * tile), T, flag);
+    else collide<L, COLL, LES>(f, a.tau, a, a.bc + (tid + (uint64_t)T * K * tile), T, flag, active, cl, fbuf);
     if constexpr (LES == kLesLearned) {
         if (!active) return;
     }
@@ -914,18 +954,18 @@ __device__ __forceinline__ void tile_step(const StepArgs& a, const uint32_t tile
     // ---- store
     if constexpr (!ESO) {
         S* po = fout + own;
-        static_for<0, Q>([&](auto qc) { P::st(po + (int32_t)(T * qc.value), f[qc.value]); });
+        static_for<0, Q>([&](auto qc) { st(po + (int32_t)(T * qc.value), f[qc.value]); });
     } else {
         const bool ev = a.even != 0;
         S* foA = fout + (ev ? 0u : T);
         S* foB = fout + (ev ? T : 0u);
-        P::st(fout + own, f[0]);
+        st(fout + own, f[0]);
         static_for<1, Q - 1, 2>([&](auto qc) {
             constexpr int pos = qc.value, neg = pos + 1;
             constexpr int sx = L::c(pos, 0), sy = L::c(pos, 1), sz = L::c(pos, 2);
             const int32_t o = own + dp[0][sx + 1] + dp[1][sy + 1] + dp[2][sz + 1];
-            P::st(foB + o + (int32_t)(T * pos), f[pos]);
-            P::st(foA + own + (int32_t)(T * pos), f[neg]);
+            st(foB + o + (int32_t)(T * pos), f[pos]);
+            st(foA + own + (int32_t)(T * pos), f[neg]);
         });
     }
 }
@@ -938,11 +978,11 @@ __device__ __forceinline__ void tile_step(const StepArgs& a, const uint32_t tile
 #define LBM_TILE_MIN_BLOCKS_HEAVY 3
 #endif
 
-template <class L, int METHOD, bool F16C, int COLL, int LES>
+template <class L, int METHOD, bool F16C, int COLL, int LES, bool FAST = false>
 __global__ void __launch_bounds__(256, (L::Q == 9) ? 5 : ((COLL == LBM_KBC || L::Q == 27) ? LBM_TILE_MIN_BLOCKS_HEAVY : LBM_TILE_MIN_BLOCKS))
     step_kernel_tile(const StepArgs a) {
     static_assert(LES != kLesLearned, "the learned closure runs in step_kernel_learned");
-    tile_step<L, METHOD, F16C, COLL, LES>(a, blockIdx.x, threadIdx.x);
+    tile_step<L, METHOD, F16C, COLL, LES, FAST>(a, blockIdx.x, threadIdx.x);
 }
 
 #ifndef LBM_LEARNED_MIN_BLOCKS
@@ -989,6 +1029,13 @@ cudaError_t launch_step(const StepArgs& a, int threads, cudaStream_t s) {
 template <class L, int METHOD, bool F16C, int COLL, int LES>
 cudaError_t launch_step_tile(const StepArgs& a, int, cudaStream_t s) {
     step_kernel_tile<L, METHOD, F16C, COLL, LES><<<a.lay.ncells / kTileCells, kTileCells, 0, s>>>(a);
+    return cudaGetLastError();
+}
+
+// The fast-arithmetic build of the block-per-tile kernel (LBM_ARITH_FAST).
+template <class L, int METHOD, bool F16C, int COLL, int LES>
+cudaError_t launch_step_tile_fast(const StepArgs& a, int, cudaStream_t s) {
+    step_kernel_tile<L, METHOD, F16C, COLL, LES, true><<<a.lay.ncells / kTileCells, kTileCells, 0, s>>>(a);
     return cudaGetLastError();
 }
 

@@ -15,6 +15,7 @@ from mojo_lbm_gb300 import (DoubleBufferConfig, EsotericPullConfig, Flags, LBM_C
                             get_D2Q9, get_D3Q19, get_D3Q27, tau_from_Re)
 from mojo_lbm_gb300 import preprocess
 from mojo_lbm_gb300.geometry import get_q_for_sphere
+from tests.conftest import needs_reference, reference_root
 
 HEADER = Path(__file__).resolve().parents[1] / "include" / "lbm_gb300.h"
 
@@ -102,13 +103,21 @@ def test_validate_edges():
     assert check(_capi.lbm_grid_t(0, 65536, 65536, 1, 16, 16, 1)) == _capi.LBM_EINVAL
     assert b"2^32" in lib.lbm_last_error()
     assert check(_capi.lbm_grid_t(0, 65536, 65520, 1, 16, 16, 1)) == 0
-    # Cs: NaN is refused in every configuration, a negative value with LES
+    # Cs is read only with LES: there a NaN or a negative value is refused, without LES any value
     g = _capi.lbm_grid_t(1, 16, 16, 16, 8, 8, 4)
-    for les, cs, ok in ((False, float("nan"), False), (True, float("nan"), False), (True, -0.1, False),
+    for les, cs, ok in ((False, float("nan"), True), (True, float("nan"), False), (True, -0.1, False),
                         (False, -0.1, True), (True, 0.0, True)):
         cc = DoubleBufferConfig(LES=les).to_c()
         cc.Cs = cs
         assert (check(g, cc) == 0) == ok, (les, cs)
+    # arithmetic: LBM_ARITH_EXACT (0) or LBM_ARITH_FAST (1)
+    for ar, ok in ((0, True), (1, True), (2, False), (-1, False)):
+        cc = DoubleBufferConfig().to_c()
+        cc.arithmetic = ar
+        assert (check(g, cc) == 0) == ok, ar
+    assert DoubleBufferConfig(arithmetic="fast").to_c().arithmetic == 1
+    with pytest.raises(ValueError):
+        DoubleBufferConfig(arithmetic="approximate")
 
 
 def test_handle_calls_reject_null():
@@ -195,11 +204,8 @@ def test_sphere_link_parameter():
 
 def test_flags_and_config_defaults_match_reference_fixture():
     """The node flags (package, C header) and LBM_Config's keyword defaults (package and
-    lbm_config_default) are the reference's, as extracted into tests/golden/constants.json; where
-    the reference is present, extracting it again gives the same fixture."""
-    import importlib.util
+    lbm_config_default) are the reference's, as extracted into tests/golden/constants.json."""
     import json
-    import os
     golden = Path(__file__).with_name("golden")
     fix = json.loads((golden / "constants.json").read_text())
     header = HEADER.read_text()
@@ -218,9 +224,18 @@ def test_flags_and_config_defaults_match_reference_fixture():
     # BCs = {} is the reference's default, to which it always adds FLUID and SOLID
     assert d["BCs"] == [] and py.INCLUDED_BCs == {Flags.FLUID, Flags.SOLID} and c.include_equilibrium_bc == 0
     assert d["f_dtype"] is None and py.f_dtype is None
-    ref = Path(os.environ.get("REF", "/root/reference"))
-    if (ref / fix["flags_source"]).exists() and (ref / fix["config_source"]).exists():
-        spec = importlib.util.spec_from_file_location("make_constants_fixture", golden / "make_constants_fixture.py")
-        mod = importlib.util.module_from_spec(spec)
-        spec.loader.exec_module(mod)
-        assert mod.extract((ref / fix["flags_source"]).read_text(), (ref / fix["config_source"]).read_text()) == fix
+
+
+@needs_reference
+def test_constants_fixture_reextracts_from_reference():
+    """Extracting the flags and LBM_Config defaults again from the reference at REF gives the
+    committed fixture."""
+    import importlib.util
+    import json
+    golden = Path(__file__).with_name("golden")
+    fix = json.loads((golden / "constants.json").read_text())
+    ref = reference_root()
+    spec = importlib.util.spec_from_file_location("make_constants_fixture", golden / "make_constants_fixture.py")
+    mod = importlib.util.module_from_spec(spec)
+    spec.loader.exec_module(mod)
+    assert mod.extract((ref / fix["flags_source"]).read_text(), (ref / fix["config_source"]).read_text()) == fix

@@ -1,6 +1,7 @@
 """Error of the GPU step against the float64 oracle, and mass drift, on 64^3 replicas of the
 D3Q19 SRT float32 lid-driven cube at Re = 100 and of the D3Q27 KBC + Smagorinsky Float16C
-esoteric-pull lid-driven cube at Re = 10000.
+esoteric-pull lid-driven cube at Re = 10000, each in the exact arithmetic (the reference's operation
+order) and in the fast arithmetic (LBM_ARITH_FAST), plus the D3Q19 Float16C cube in the fast one.
 
 The GPU runs in its own arithmetic and storage (float32, or Float16C codes with DDF shift); the
 oracle runs the same configuration in float64 arithmetic and float64 storage from the same
@@ -25,11 +26,16 @@ pytestmark = pytest.mark.gpu
 N = 64
 U = 0.1
 CASES = {
-    # name: lattice, method, collision, LES, Float16C, Re, steps, (max |du|/U bound, rel L2 bound), mass bound
+    # name: lattice, method, collision, LES, Float16C, Re, steps, (max |du|/U bound, rel L2 bound), mass bound,
+    #       arithmetic
     # float32: the population error grows ~2e-8 per step with the float32 mass drift (rounding)
-    "d3q19_srt_fp32_re100": ("D3Q19", "db", "SRT", False, False, 100.0, 200, (5e-5, 1e-5), 1e-5),
+    "d3q19_srt_fp32_re100": ("D3Q19", "db", "SRT", False, False, 100.0, 200, (5e-5, 1e-5), 1e-5, "exact"),
+    "d3q19_srt_fp32_re100_fast": ("D3Q19", "db", "SRT", False, False, 100.0, 200, (5e-5, 1e-5), 1e-5, "fast"),
+    "d3q19_srt_f16c_re100_fast": ("D3Q19", "db", "SRT", False, True, 100.0, 200, (2e-2, 2e-4), 1e-5, "fast"),
     # Float16C at tau = 0.5019: differences of one storage unit grow in the nearly inviscid flow
-    "d3q27_kbc_les_f16c_eso_re1e4": ("D3Q27", "eso", "KBC", True, True, 10000.0, 200, (5e-2, 2e-4), 1e-5),
+    "d3q27_kbc_les_f16c_eso_re1e4": ("D3Q27", "eso", "KBC", True, True, 10000.0, 200, (5e-2, 2e-4), 1e-5, "exact"),
+    "d3q27_kbc_les_f16c_eso_re1e4_fast": ("D3Q27", "eso", "KBC", True, True, 10000.0, 200, (5e-2, 2e-4), 1e-5,
+                                          "fast"),
 }
 
 
@@ -48,11 +54,11 @@ def _u_max_err(grid, cfg, f_gpu_dec, f64, bc64, flags, fluid, after_odd):
 
 @pytest.mark.parametrize("name", list(CASES))
 def test_error_against_float64_oracle_and_mass_drift(name):
-    lat, meth, coll, les, f16, Re, steps, (u_bound, l2_bound), mass_bound = CASES[name]
+    lat, meth, coll, les, f16, Re, steps, (u_bound, l2_bound), mass_bound, arith = CASES[name]
     tile = (8, 8, 4) if lat == "D3Q19" else (4, 8, 8)
     grid = make_grid(lat, (N, N, N), tile)
     method = LBM_method.DOUBLE_BUFFER if meth == "db" else LBM_method.ESOTERIC_PULL
-    cfg = LBM_Config(method, collision_op=coll, LES=les, DDF_shift=f16, use_float16c=f16)
+    cfg = LBM_Config(method, collision_op=coll, LES=les, DDF_shift=f16, use_float16c=f16, arithmetic=arith)
     cfg64 = LBM_Config(method, collision_op=coll, LES=les, DDF_shift=f16)  # float64 storage, same shift
     flags, bc = ldc_flags(grid, cfg, U)
     tau = 3.0 * U * (N - 1) / Re + 0.5
@@ -63,6 +69,7 @@ def test_error_against_float64_oracle_and_mass_drift(name):
     oracle.init(cfg64, grid, 64, f64)
     f64b = f64.copy()
     solver = Solver(grid, cfg)
+    assert arith == "exact" or solver.kernel_path == 2  # the fast arithmetic runs in the block-per-tile kernel
     fa, bct, flt = to_dev(f0), to_dev(bc), to_dev(flags)
     fb = fa.clone()
     bc64 = bc.astype(np.float64)
