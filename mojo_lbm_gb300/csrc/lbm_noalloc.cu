@@ -9,8 +9,10 @@
 // its scratch (one float64 x 4 partial per block of 4096 cells, plus the 4 results) lives in the
 // file-scope device array below, which every GPU that loads the library holds until the process
 // exits.  That bounds the grid to kNoAllocMaxCells cells.  The first call on a device looks the
-// array up with cudaGetSymbolAddress, so it should come before any stream capture.  Every call
-// shares the array: calls that overlap on the GPU race.
+// array up with cudaGetSymbolAddress, so it should come before any stream capture; the address is
+// kept for the rest of the process, so the entry point must not be used on a device after a
+// cudaDeviceReset of that device (the array then lives at a new address).  Every call shares the
+// array: calls that overlap on the GPU race.
 #include <cuda_runtime.h>
 
 #include <cmath>
@@ -20,7 +22,8 @@
 #include "lbm_aux.cuh"
 
 namespace lbm {
-void set_last_error(const char* msg);  // lbm_capi.cu
+void set_last_error(const char* msg);         // lbm_capi.cu
+LayoutDesc make_layout(const lbm_grid_t& g);  // lbm_capi.cu
 }
 
 using namespace lbm;
@@ -37,7 +40,8 @@ constexpr uint64_t kNoAllocMaxCells = (uint64_t)kMaxPartials * kChunkCells;  // 
 // Host code must not use this name as an address; it goes through noalloc_scratch().
 static __device__ __align__(256) double g_noalloc_scratch[kMaxPartials * 4 + 4];
 
-// Device address of g_noalloc_scratch on the current device, looked up once per device.
+// Device address of g_noalloc_scratch on the current device, looked up once per device and kept
+// (valid until a cudaDeviceReset of that device).
 std::mutex g_noalloc_mutex;
 constexpr int kMaxDevices = 64;
 double* g_noalloc_ptr[kMaxDevices] = {};
@@ -130,16 +134,7 @@ extern "C" lbm_status lbm_reduce_mass_momentum_noalloc(const lbm_config_t* cfg, 
         return nfail(LBM_ECUDA, std::string("cudaGetSymbolAddress(scratch): ") + cudaGetErrorString(e));
 
     ChunkArgs a;
-    a.lay.nx = grid->nx; a.lay.ny = grid->ny; a.lay.nz = grid->nz;
-    a.lay.tx = grid->tx; a.lay.ty = grid->ty; a.lay.tz = grid->tz;
-    a.lay.ntx = grid->nx / grid->tx; a.lay.nty = grid->ny / grid->ty; a.lay.ntz = grid->nz / grid->tz;
-    a.lay.T = (uint32_t)(grid->tx * grid->ty * grid->tz);
-    a.lay.ncells = (uint32_t)N;
-    a.lay.d_tx = FastDiv((uint32_t)grid->tx);
-    a.lay.d_ty = FastDiv((uint32_t)grid->ty);
-    a.lay.d_T = FastDiv(a.lay.T);
-    a.lay.d_ntx = FastDiv((uint32_t)a.lay.ntx);
-    a.lay.d_nty = FastDiv((uint32_t)a.lay.nty);
+    a.lay = make_layout(*grid);
     a.f = f;
     a.flags = flags;
     a.partial = scratch;

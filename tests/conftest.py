@@ -1,3 +1,5 @@
+from __future__ import annotations
+
 import sys
 from pathlib import Path
 
@@ -25,6 +27,17 @@ def pytest_collection_modifyitems(config, items):
     for item in items:
         if "gpu" in item.keywords:
             item.add_marker(skip)
+
+
+def reference_root() -> Path | None:
+    """The reference checkout named by the REF environment variable, or None when it is unset."""
+    import os
+    ref = os.environ.get("REF")
+    return Path(ref) if ref else None
+
+
+needs_reference = pytest.mark.skipif(reference_root() is None,
+                                     reason="REF (the reference checkout) is not set")
 
 
 @pytest.fixture(scope="session")

@@ -1,13 +1,14 @@
 """Extracts two tables of the reference into constants.json: the node flags of struct Flags
 (src/lbm/constants.mojo: the low-nibble enum and the high-bit masks) and the keyword defaults of
-LBM_Config.__init__ (src/lbm/config.mojo).  Run in a checkout that has the reference at REF
-(default /root/reference)."""
+LBM_Config.__init__ (src/lbm/config.mojo).  Run in a checkout that has the reference at REF (an
+environment variable; the script stops when it is unset)."""
 import json
 import os
+import sys
 import re
 from pathlib import Path
 
-REF = Path(os.environ.get("REF", "/root/reference"))
+REF = Path(os.environ["REF"]) if os.environ.get("REF") else None  # the reference checkout
 FLAGS_SRC = "src/lbm/constants.mojo"
 CONFIG_SRC = "src/lbm/config.mojo"
 OUT = Path(__file__).with_name("constants.json")
@@ -56,6 +57,8 @@ def extract(flags_text: str, config_text: str) -> dict:
 
 
 def main():
+    if REF is None:
+        sys.exit("set REF to the root of a reference checkout")
     fix = extract((REF / FLAGS_SRC).read_text(), (REF / CONFIG_SRC).read_text())
     OUT.write_text(json.dumps(fix, indent=1) + "\n")
     print(f"wrote {OUT}: {fix['flags']} {fix['config_defaults']}")

@@ -1,14 +1,14 @@
 """Extracts the DFG (Schäfer-Turek) 2D cylinder benchmark at Re = 20 as the reference records it in
 benchmarks/Cylinder2D/CylinderFlow_Re20.mojo: the target drag and lift coefficients and the drag
 and lift the reference itself reached at each resolution, into dfg_re20.json.  Run in a checkout
-that has the reference at REF (default /root/reference)."""
+that has the reference at REF (an environment variable; the script stops when it is unset)."""
 import json
 import os
 import re
 import sys
 from pathlib import Path
 
-REF = Path(os.environ.get("REF", "/root/reference"))
+REF = Path(os.environ["REF"]) if os.environ.get("REF") else None  # the reference checkout
 SRC = "benchmarks/Cylinder2D/CylinderFlow_Re20.mojo"
 OUT = Path(__file__).with_name("dfg_re20.json")
 
@@ -39,6 +39,8 @@ def extract(text: str) -> dict:
 
 
 def main() -> int:
+    if REF is None:
+        sys.exit("set REF to the root of a reference checkout")
     fix = extract((REF / SRC).read_text())
     OUT.write_text(json.dumps(fix, indent=1))
     print(f"wrote {OUT}: Cd {fix['Cd']}, Cl {fix['Cl']}, {len(fix['reference_runs'])} recorded runs")

@@ -1,12 +1,12 @@
 """Extracts the Re = 100 column of the Ghia, Ghia & Shin (1982) cavity centre-line tables that the
 reference ships (benchmarks/LDC/u_velocity_results.txt, benchmarks/LDC/v_velocity_results.csv)
-into ghia_re100.json.  Run in a checkout that has the reference at REF (default /root/reference)."""
+into ghia_re100.json.  Run in a checkout that has the reference at REF (an environment variable; the script stops when it is unset)."""
 import json
 import os
 import sys
 from pathlib import Path
 
-REF = Path(os.environ.get("REF", "/root/reference"))
+REF = Path(os.environ["REF"]) if os.environ.get("REF") else None  # the reference checkout
 OUT = Path(__file__).with_name("ghia_re100.json")
 
 
@@ -18,6 +18,8 @@ def column(path: Path, sep: str | None):
 
 
 def main() -> int:
+    if REF is None:
+        sys.exit("set REF to the root of a reference checkout")
     u = column(REF / "benchmarks/LDC/u_velocity_results.txt", None)
     v = column(REF / "benchmarks/LDC/v_velocity_results.csv", ",")
     OUT.write_text(json.dumps({"source": "benchmarks/LDC/u_velocity_results.txt, v_velocity_results.csv (Re=100)",

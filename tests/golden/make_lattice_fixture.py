@@ -2,13 +2,14 @@
 the directions in the reference's order (rest first, each direction followed by its opposite) and
 the weights as the numerator / denominator pairs the reference writes, and the order of the
 symmetric stress components (get_stress_indices) for D = 2 and 3, into lattices.json.  Run in a
-checkout that has the reference at REF (default /root/reference)."""
+checkout that has the reference at REF (an environment variable; the script stops when it is unset)."""
 import json
 import os
+import sys
 import re
 from pathlib import Path
 
-REF = Path(os.environ.get("REF", "/root/reference"))
+REF = Path(os.environ["REF"]) if os.environ.get("REF") else None  # the reference checkout
 SRC = "src/lbm/lattice.mojo"
 OUT = Path(__file__).with_name("lattices.json")
 NAMES = ("D2Q9", "D3Q19", "D3Q27")
@@ -52,6 +53,8 @@ def extract(text: str) -> dict:
 
 
 def main():
+    if REF is None:
+        sys.exit("set REF to the root of a reference checkout")
     fix = extract((REF / SRC).read_text())
     OUT.write_text(json.dumps(fix, indent=1) + "\n")
     print(f"wrote {OUT}: " + ", ".join(f"{n} {len(fix[n]['directions'])}" for n in NAMES))

@@ -10,6 +10,7 @@ import pytest
 
 import oracle
 from mojo_lbm_gb300 import Flags, LBM_Config, LBM_method, get_D2Q9, get_D3Q19, get_D3Q27
+from tests.conftest import needs_reference, reference_root
 from tests.lbm_cases import initial_f, ldc_flags, make_grid, mixed_flags
 
 GOLDEN = Path(__file__).with_name("golden")
@@ -229,21 +230,13 @@ def test_ldc_re100_against_ghia_fixture():
 # ---- the reference's DFG cylinder record (tests/golden/dfg_re20.json) --------------------------
 def test_dfg_fixture():
     """The fixture holds the DFG targets and the reference's recorded drag for the resolutions the
-    GPU test runs; where the reference is present, extracting it again gives the same fixture."""
-    import importlib.util
-    import os
+    GPU test runs (test_fixture_reextracts_from_reference re-extracts it where REF is set)."""
     fix = json.loads((GOLDEN / "dfg_re20.json").read_text())
     assert abs(fix["Cd"] - 5.58) < 0.01 and 0.0 < fix["Cl"] < 0.02
     grids = {tuple(r["grid"]) for r in fix["reference_runs"]}
     assert {(1024, 256), (2560, 512)} <= grids
     for r in fix["reference_runs"]:
         assert abs(r["drag"] - fix["Cd"]) / fix["Cd"] < 0.02
-    src = Path(os.environ.get("REF", "/root/reference")) / fix["source"]
-    if src.exists():
-        spec = importlib.util.spec_from_file_location("make_dfg_fixture", GOLDEN / "make_dfg_fixture.py")
-        mod = importlib.util.module_from_spec(spec)
-        spec.loader.exec_module(mod)
-        assert mod.extract(src.read_text()) == fix
 
 
 # ---- the oracle's own goldens (tests/golden/oracle_goldens.json) --------------------------------
@@ -274,9 +267,7 @@ def test_oracle_goldens():
 def test_lattices_match_reference_fixture(lid, name, pylat):
     """The oracle's and the package's velocity sets are the reference's: the directions in its order,
     the weights equal to its fractions as float32 (the reference's float_dtype) and the order of the
-    stress components; where the reference is present, extracting it again gives the same fixture."""
-    import importlib.util
-    import os
+    stress components (test_fixture_reextracts_from_reference re-extracts it where REF is set)."""
     fix = json.loads((GOLDEN / "lattices.json").read_text())
     ref = fix[name]
     c, w, o = oracle.lattice(lid)
@@ -288,9 +279,16 @@ def test_lattices_match_reference_fixture(lid, name, pylat):
     assert np.array_equal(w.astype(np.float32), wref) and np.array_equal(L.weights.astype(np.float32), wref)
     assert all(np.array_equal(dirs[q], -dirs[q + 1]) and o[q] == q + 1 for q in range(1, L.Q, 2))
     assert [list(p) for p in L.stress_indices] == oracle.stress_pairs(L.D) == fix["stress_pairs"][str(L.D)]
-    src = Path(os.environ.get("REF", "/root/reference")) / fix["source"]
-    if src.exists():
-        spec = importlib.util.spec_from_file_location("make_lattice_fixture", GOLDEN / "make_lattice_fixture.py")
-        mod = importlib.util.module_from_spec(spec)
-        spec.loader.exec_module(mod)
-        assert mod.extract(src.read_text()) == fix
+
+
+@needs_reference
+@pytest.mark.parametrize("name,script", [("dfg_re20.json", "make_dfg_fixture.py"),
+                                         ("lattices.json", "make_lattice_fixture.py")])
+def test_fixture_reextracts_from_reference(name, script):
+    """Extracting the fixture again from the reference at REF gives the committed file."""
+    import importlib.util
+    fix = json.loads((GOLDEN / name).read_text())
+    spec = importlib.util.spec_from_file_location(script[:-3], GOLDEN / script)
+    mod = importlib.util.module_from_spec(spec)
+    spec.loader.exec_module(mod)
+    assert mod.extract((reference_root() / fix["source"]).read_text()) == fix

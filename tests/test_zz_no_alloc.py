@@ -31,23 +31,52 @@ def noalloc(cfg, grid, f, flags, after_odd: bool):
     return np.array(out[:])
 
 
-CASES = [("D3Q19", (64, 48, 40), (8, 8, 4), LBM_method.DOUBLE_BUFFER, False),
-         ("D2Q9", (96, 80, 1), (16, 16, 1), LBM_method.ESOTERIC_PULL, True)]
+# every lattice x storage x streaming method appears; the cell counts are not multiples of 4096
+# (the entry point's block), so each case's last block is partly filled
+CASES = [("D3Q19", (56, 48, 40), (8, 8, 4), LBM_method.DOUBLE_BUFFER, False),
+         ("D2Q9", (96, 80, 1), (16, 16, 1), LBM_method.ESOTERIC_PULL, True),
+         ("D3Q27", (40, 24, 20), (8, 8, 4), LBM_method.ESOTERIC_PULL, False),
+         ("D3Q19", (40, 24, 20), (8, 8, 4), LBM_method.ESOTERIC_PULL, True),
+         ("D2Q9", (112, 48, 1), (16, 16, 1), LBM_method.DOUBLE_BUFFER, False),
+         ("D3Q27", (24, 16, 40), (8, 8, 4), LBM_method.DOUBLE_BUFFER, True)]
+
+
+def _case(lat, shape, tile, meth, f16, seed):
+    grid = make_grid(lat, shape, tile)
+    cfg = LBM_Config(meth, DDF_shift=f16, use_float16c=f16)
+    flags, bc = ldc_flags(grid, cfg, 0.1)
+    f0 = initial_f(grid, cfg, np.random.default_rng(seed), amp=0.04)
+    f = torch.from_numpy(f0.view(np.int16) if f16 else f0).cuda()
+    fl = torch.from_numpy(flags).cuda()
+    return grid, cfg, f, fl
 
 
 def test_noalloc_matches_handle_reduction_twice_in_a_row():
-    """Two different grids, one after the other: the second call must not see the first call's
-    partials left in the shared array."""
-    for lat, shape, tile, meth, f16 in CASES:
-        grid = make_grid(lat, shape, tile)
-        cfg = LBM_Config(meth, DDF_shift=f16, use_float16c=f16)
-        flags, bc = ldc_flags(grid, cfg, 0.1)
-        f0 = initial_f(grid, cfg, np.random.default_rng(31), amp=0.04)
-        f = torch.from_numpy(f0.view(np.int16) if f16 else f0).cuda()
-        fl = torch.from_numpy(flags).cuda()
+    """Six grids one after the other, each reduced twice in a row: no call may see the partials
+    an earlier call left in the shared array."""
+    for i, (lat, shape, tile, meth, f16) in enumerate(CASES):
+        assert (shape[0] * shape[1] * shape[2]) % 4096 != 0
+        grid, cfg, f, fl = _case(lat, shape, tile, meth, f16, 31 + i)
         ref = np.array(Solver(grid, cfg).mass_momentum(f, fl, after_odd_step=True))
-        got = noalloc(cfg, grid, f, fl, True)
-        np.testing.assert_allclose(got, ref, rtol=1e-12, atol=1e-9 * abs(ref[0]))
+        for _ in range(2):
+            got = noalloc(cfg, grid, f, fl, True)
+            np.testing.assert_allclose(got, ref, rtol=1e-12, atol=1e-9 * abs(ref[0]))
+
+
+def test_noalloc_at_its_maximum_size():
+    """A grid of exactly 2^27 cells (the most the fixed scratch covers) is accepted and matches the
+    handle-based reduction.  D2Q9 Float16C, periodic, from a rest equilibrium set on the device."""
+    grid = make_grid("D2Q9", (16384, 8192, 1), (16, 16, 1))
+    cfg = LBM_Config(LBM_method.DOUBLE_BUFFER, DDF_shift=True, use_float16c=True)
+    f = torch.empty(grid.num_points * grid.Q, dtype=torch.int16, device="cuda")
+    fl = torch.zeros(grid.num_points, dtype=torch.uint8, device="cuda")
+    s = Solver(grid, cfg)
+    s.init_equilibrium(f)
+    ref = np.array(s.mass_momentum(f, fl))
+    s.close()
+    got = noalloc(cfg, grid, f, fl, False)
+    np.testing.assert_allclose(got, ref, rtol=1e-12, atol=1e-9 * abs(ref[0]))
+    assert ref[0] == pytest.approx(grid.num_points, rel=1e-6)
 
 
 def test_noalloc_rejects_grids_beyond_its_scratch():
