@@ -147,12 +147,16 @@ lbm_status lbm_set_block_threads(lbm_handle* h, int32_t threads);
 
 /* Kernel choice (no counterpart in the reference, which compiles one kernel per layout):
  * 0 = automatic (default), 1 = the generic kernel (any tile), 2 = the block-per-tile kernel,
- * which needs 256-cell tiles with power-of-two sides and Q*N < 2^31 (LBM_EUNSUPPORTED
- * otherwise).  With LBM_ARITH_EXACT both produce identical populations; the generic kernel
- * always computes the exact arithmetic. */
+ * which needs 256-cell tiles with power-of-two sides and Q*N < 2^31, 3 = the cell-pair
+ * block-per-tile kernel (one thread per two cells along x, word-wide population accesses), which
+ * also needs the double-buffer method and tx >= 2 (LBM_EUNSUPPORTED otherwise); a step whose
+ * population buffers are not 8-byte aligned, or a handle with the learned closure, runs the
+ * block-per-tile kernel instead.  With LBM_ARITH_EXACT all produce identical populations; the
+ * generic kernel always computes the exact arithmetic. */
 lbm_status lbm_set_kernel_path(lbm_handle* h, int32_t path);
 
-/* The kernel lbm_*_step will use: 1 generic, 2 block-per-tile, -1 for a null handle. */
+/* The kernel lbm_*_step will use (aligned buffers): 1 generic, 2 block-per-tile, 3 cell-pair,
+ * -1 for a null handle. */
 int32_t lbm_kernel_path(const lbm_handle* h);
 
 /* ---- the step ---- */

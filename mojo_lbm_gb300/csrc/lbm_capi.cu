@@ -23,6 +23,9 @@ StepLaunch get_tile_step_d3q27(int, int, int, int);
 StepLaunch get_fast_tile_step_d2q9(int, int, int, int);
 StepLaunch get_fast_tile_step_d3q19(int, int, int, int);
 StepLaunch get_fast_tile_step_d3q27(int, int, int, int);
+StepLaunch get_pair_step_d2q9(int, int, int, int);
+StepLaunch get_pair_step_d3q19(int, int, int, int);
+StepLaunch get_pair_step_d3q27(int, int, int, int);
 StepLaunch get_learned_step_d2q9(int, int, int);
 StepLaunch get_learned_step_d3q19(int, int, int);
 StepLaunch get_learned_step_d3q27(int, int, int);
@@ -99,7 +102,8 @@ struct lbm_handle {
     StepLaunch step;       // generic kernel (any tile)
     StepLaunch step_tile;  // block-per-tile kernel, or null when the grid does not qualify
     StepLaunch step_learned;  // block-per-tile kernel with the learned closure (LES handles), or null
-    int path;              // 0 auto, 1 generic only, 2 block-per-tile only
+    StepLaunch step_pair;  // cell-pair block-per-tile kernel (double buffer, tx >= 2), or null
+    int path;              // 0 auto, 1 generic only, 2 block-per-tile only, 3 cell-pair
     uint8_t* box_sum;      // per warp box (32 cells): summary byte (flags other than 0 inside, on faces)
     uint2* cell_masks;     // per cell: neighbour-solid masks, written for the warps with a mask bit set
     uint8_t* flags_seen;   // the flags the summary was built from
@@ -173,10 +177,18 @@ StepArgs step_args(const lbm_handle* h, const void* f_in, void* f_out, float* bc
 
 bool use_tile(const lbm_handle* h) { return h->step_tile != nullptr && h->path != 1; }
 
-// The kernel the next step runs.
-StepLaunch step_fn(const lbm_handle* h) {
+// The cell-pair kernel is chosen (path 3) and can run: no learned closure.
+bool use_pair(const lbm_handle* h) { return h->path == 3 && h->step_pair != nullptr && !h->closure_on; }
+
+// The kernel the next step with these arguments runs.  The cell-pair kernel moves 8-byte
+// (float32) or 4-byte (Float16C) words, so it needs 8-byte aligned population buffers; others
+// take the per-cell block-per-tile kernel.
+StepLaunch step_fn(const lbm_handle* h, const StepArgs& a) {
     if (!use_tile(h)) return h->step;
-    return h->closure_on ? h->step_learned : h->step_tile;
+    if (h->closure_on) return h->step_learned;
+    if (use_pair(h) && ((reinterpret_cast<uintptr_t>(a.f_in) | reinterpret_cast<uintptr_t>(a.f_out)) & 7u) == 0u)
+        return h->step_pair;
+    return h->step_tile;
 }
 
 // Brings the per-tile warp masks of the block-per-tile kernel up to date with `flags`: the boxes
@@ -222,7 +234,7 @@ lbm_status step_once(lbm_handle* h, const void* f_in, void* f_out, float* bc, co
             if (st != LBM_OK) return st;
         }
     }
-    LBM_CK(step_fn(h)(a, h->threads, s));
+    LBM_CK(step_fn(h, a)(a, h->threads, s));
     return LBM_OK;
 }
 
@@ -328,6 +340,10 @@ lbm_status lbm_create(const lbm_config_t* cfg, const lbm_grid_t* grid, lbm_handl
                     : grid->lattice == LBM_D2Q9 ? get_learned_step_d2q9(m, f16, co)
                     : grid->lattice == LBM_D3Q19 ? get_learned_step_d3q19(m, f16, co)
                                                  : get_learned_step_d3q27(m, f16, co);
+    h->step_pair = !(tile_ok && m == LBM_DOUBLE_BUFFER && grid->tx >= 2) ? nullptr
+                 : grid->lattice == LBM_D2Q9 ? get_pair_step_d2q9(f16, co, les, fast)
+                 : grid->lattice == LBM_D3Q19 ? get_pair_step_d3q19(f16, co, les, fast)
+                                              : get_pair_step_d3q27(f16, co, les, fast);
     h->path = 0;
     h->ntiles = h->lay.ncells / h->lay.T;
     h->mx = (uint32_t)grid->tx - 1u;
@@ -420,16 +436,20 @@ lbm_status lbm_set_block_threads(lbm_handle* h, int32_t threads) {
 
 lbm_status lbm_set_kernel_path(lbm_handle* h, int32_t path) {
     if (check_handle(h)) return LBM_EINVAL;
-    if (path < 0 || path > 2) return fail(LBM_EINVAL, "path must be 0 (auto), 1 (generic) or 2 (block-per-tile)");
+    if (path < 0 || path > 3)
+        return fail(LBM_EINVAL, "path must be 0 (auto), 1 (generic), 2 (block-per-tile) or 3 (cell-pair)");
     if (path == 2 && !h->step_tile)
         return fail(LBM_EUNSUPPORTED, "the block-per-tile kernel needs 256-cell power-of-two tiles and Q*N < 2^31");
+    if (path == 3 && !h->step_pair)
+        return fail(LBM_EUNSUPPORTED, "the cell-pair kernel needs the double-buffer method, 256-cell power-of-two "
+                                      "tiles with tx >= 2 and Q*N < 2^31");
     if (path == 1 && h->closure_on)
         return fail(LBM_EUNSUPPORTED, "the learned closure runs in the block-per-tile kernel only");
     h->path = path;
     return LBM_OK;
 }
 
-int32_t lbm_kernel_path(const lbm_handle* h) { return h ? (use_tile(h) ? 2 : 1) : -1; }
+int32_t lbm_kernel_path(const lbm_handle* h) { return h ? (use_tile(h) ? (use_pair(h) ? 3 : 2) : 1) : -1; }
 
 lbm_status lbm_double_buffer_step(lbm_handle* h, void* f_out, const void* f_in, float* bc, const uint8_t* flags,
                                   float tau, void* stream) {
@@ -483,7 +503,7 @@ lbm_status lbm_run(lbm_handle* h, void* f_a, void* f_b, float* bc, const uint8_t
     if (n_steps >= chunk) {
         uint32_t tau_bits;
         std::memcpy(&tau_bits, &tau, 4);
-        const GraphKey key{f_a, f_b, bc, flags, tau_bits, (int)(first_step % 2), chunk, use_tile(h) ? 2 : 1};
+        const GraphKey key{f_a, f_b, bc, flags, tau_bits, (int)(first_step % 2), chunk, use_tile(h) ? (use_pair(h) ? 3 : 2) : 1};
         auto it = h->graphs.find(key);
         if (it == h->graphs.end()) {
             cudaGraph_t g = nullptr;
@@ -494,7 +514,7 @@ lbm_status lbm_run(lbm_handle* h, void* f_a, void* f_b, float* bc, const uint8_t
                 const StepArgs a = eso ? step_args(h, f_a, f_a, bc, flags, tau, a_is_src ? 1 : 0)
                                        : (a_is_src ? step_args(h, f_a, f_b, bc, flags, tau, 0)
                                                    : step_args(h, f_b, f_a, bc, flags, tau, 0));
-                const StepLaunch fn = step_fn(h);
+                const StepLaunch fn = step_fn(h, a);
                 if (fn(a, h->threads, h->capture_stream) != cudaSuccess) st = LBM_ECUDA;
             }
             cudaError_t e = cudaStreamEndCapture(h->capture_stream, &g);

@@ -1070,6 +1070,12 @@ cudaError_t launch_step_learned(const StepArgs& a, int, cudaStream_t s) {
 
 inline int step_index(int method, int f16c, int coll, int les) { return ((method * 2 + f16c) * 4 + coll) * 2 + les; }
 
+// Tables of the 16 double-buffer variants of one lattice (the cell-pair and fused-link kernels),
+// indexed by (f16c*4 + collision)*2 + les.
+#define LBM_DB_TABLE(FN, L) {LBM_STEP_ROW(FN, L, LBM_DOUBLE_BUFFER, false), LBM_STEP_ROW(FN, L, LBM_DOUBLE_BUFFER, true)}
+
+inline int db_index(int f16c, int coll, int les) { return (f16c * 4 + coll) * 2 + les; }
+
 // Tables of the 16 learned-closure variants of one lattice (block-per-tile kernel), indexed by
 // (method*2 + f16c)*4 + collision.
 #define LBM_LEARNED_ROW(FN, L, M, F)                                                           \

@@ -44,7 +44,8 @@ class Solver:
         check(self._lib.lbm_set_block_threads(self._h, int(threads)))
 
     def set_kernel_path(self, path: int) -> None:
-        """0 automatic, 1 generic kernel, 2 block-per-tile kernel (identical results)."""
+        """0 automatic, 1 generic kernel, 2 block-per-tile kernel, 3 cell-pair block-per-tile kernel
+        (double buffer; identical results in the exact arithmetic)."""
         check(self._lib.lbm_set_kernel_path(self._h, int(path)))
 
     @property
