@@ -240,6 +240,25 @@ lbm_status lbm_linkwise_bounceback(lbm_handle* h, void* f, float* link_force,
                                    const float* dists, int64_t n_links, int32_t method,
                                    int32_t compute_force, float q_clamp, void* stream);
 
+/* Interpolated bounce-back fused into the step: the node-wise form of the reference's WIP kernel
+ * nodewise_bounceback_kernel (geometry/nodewise_interpolated_BB.mojo:46-185), with the
+ * interpolation of its link-wise kernel (geometry/interpolated_BB.mojo:102-141).  Registers the links
+ * (device arrays as lbm_linkwise_bounceback takes them; copied into a per-cell table, so the caller
+ * may free them) with the handle: from the next step on, every double-buffer step applies them
+ * inside the step kernel, in place of a link-wise pass after it.  A fluid cell with a link (x, i)
+ * whose wall node x + c_i is a raw SOLID flag replaces its mid-grid bounce-back value of direction
+ * opp(i) by the value the link-wise kernel would have stored at (x, i) after the previous step, and
+ * writes that link's force (c_i (f_into + f_bb), n_links*D floats, link fastest, in the caller's link
+ * order) into link_force when it is not NULL.  The lattice therefore holds the step's own values in
+ * the link slots (x, i): one lbm_linkwise_bounceback pass (method, q_clamp, no force) turns it into
+ * the lattice the link-wise path has after the same steps, and the forces written by step k are
+ * the link-wise path's of step k-1.  n_links = 0 removes the links.  Needs the block-per-tile
+ * kernel (LBM_EUNSUPPORTED otherwise); waits for the device to be idle: call it between steps.
+ * LBM_EINVAL for an id outside the grid, a direction outside [1, Q), a NaN distance or two links
+ * with the same cell and direction. */
+lbm_status lbm_set_links(lbm_handle* h, const int32_t* fluid_ids, const int32_t* dirs, const float* dists,
+                         int64_t n_links, int32_t method, float q_clamp, float* link_force, void* stream);
+
 /* RigidStationaryObject.sum_force (geometry/rigidstationary.mojo:155-169): column sums of a
  * link-force array, reduced in float64 on the device.  Synchronises the stream. */
 lbm_status lbm_sum_link_force(lbm_handle* h, const float* link_force, int64_t n_links,

@@ -38,7 +38,7 @@ def _sources() -> list[Path]:
 
 
 def _deps() -> list[Path]:
-    return _sources() + sorted(CSRC.glob("*.cuh")) + [ROOT / "include" / "lbm_gb300.h", Path(__file__)]
+    return _sources() + sorted(CSRC.glob("*.cuh")) + sorted(CSRC.glob("*.h")) + [ROOT / "include" / "lbm_gb300.h", Path(__file__)]
 
 
 def _extra_from_env() -> list[str]:

@@ -79,6 +79,7 @@ SIGNATURES = {
     "lbm_reduce_mass_momentum": (_i32, [_vp, _vp, _vp, _i32, C.POINTER(C.c_double), _vp]),
     "lbm_reduce_mass_momentum_noalloc": (_i32, [_CFG, _GRID, _vp, _vp, _i32, C.POINTER(C.c_double), _vp]),
     "lbm_linkwise_bounceback": (_i32, [_vp, _vp, _vp, _vp, _vp, _vp, _i64, _i32, _i32, _f32, _vp]),
+    "lbm_set_links": (_i32, [_vp, _vp, _vp, _vp, _i64, _i32, _f32, _vp, _vp]),
     "lbm_sum_link_force": (_i32, [_vp, _vp, _i64, C.POINTER(C.c_double), _vp]),
     "lbm_drag_force": (_i32, [_vp, _vp, _vp, _vp, _vp, _i64, _vp]),
     "lbm_batch_create": (_i32, [_CFG, _i32, _GRID, C.POINTER(_vp)]),

@@ -12,6 +12,7 @@
 #include <tuple>
 
 #include "lbm_aux.cuh"
+#include "lbm_link_tables.h"
 
 namespace lbm {
 StepLaunch get_step_d2q9(int, int, int, int);
@@ -26,6 +27,9 @@ StepLaunch get_fast_tile_step_d3q27(int, int, int, int);
 StepLaunch get_pair_step_d2q9(int, int, int, int);
 StepLaunch get_pair_step_d3q19(int, int, int, int);
 StepLaunch get_pair_step_d3q27(int, int, int, int);
+StepLaunch get_links_tile_step_d2q9(int, int, int, int);
+StepLaunch get_links_tile_step_d3q19(int, int, int, int);
+StepLaunch get_links_tile_step_d3q27(int, int, int, int);
 StepLaunch get_learned_step_d2q9(int, int, int);
 StepLaunch get_learned_step_d3q19(int, int, int);
 StepLaunch get_learned_step_d3q27(int, int, int);
@@ -103,6 +107,7 @@ struct lbm_handle {
     StepLaunch step_tile;  // block-per-tile kernel, or null when the grid does not qualify
     StepLaunch step_learned;  // block-per-tile kernel with the learned closure (LES handles), or null
     StepLaunch step_pair;  // cell-pair block-per-tile kernel (double buffer, tx >= 2), or null
+    StepLaunch step_links;    // block-per-tile kernel with fused links (double buffer), or null
     int path;              // 0 auto, 1 generic only, 2 block-per-tile only, 3 cell-pair
     uint8_t* box_sum;      // per warp box (32 cells): summary byte (flags other than 0 inside, on faces)
     uint2* cell_masks;     // per cell: neighbour-solid masks, written for the warps with a mask bit set
@@ -122,6 +127,14 @@ struct lbm_handle {
     int closure_on;
     cudaStream_t capture_stream;
     std::map<GraphKey, cudaGraphExec_t> graphs;
+    // interpolated bounce-back fused into the step (lbm_set_links)
+    uint2* link_table;     // per cell, or null
+    float* link_dist;
+    int32_t* link_id;
+    float* link_force;     // caller's, or null
+    int64_t n_links;
+    float q_clamp;
+    int bouzidi;
 };
 
 namespace lbm {
@@ -172,13 +185,22 @@ StepArgs step_args(const lbm_handle* h, const void* f_in, void* f_out, float* bc
     a.my = h->my;
     a.shx = h->shx;
     a.shxy = h->shxy;
+    a.link_table = h->link_table;
+    a.link_dist = h->link_dist;
+    a.link_id = h->link_id;
+    a.link_force = h->link_force;
+    a.link_stride = h->n_links;
+    a.q_clamp = h->q_clamp;
+    a.bouzidi = h->bouzidi;
     return a;
 }
 
 bool use_tile(const lbm_handle* h) { return h->step_tile != nullptr && h->path != 1; }
 
-// The cell-pair kernel is chosen (path 3) and can run: no learned closure.
-bool use_pair(const lbm_handle* h) { return h->path == 3 && h->step_pair != nullptr && !h->closure_on; }
+// The cell-pair kernel is chosen (path 3) and can run: no learned closure, no fused links.
+bool use_pair(const lbm_handle* h) {
+    return h->path == 3 && h->step_pair != nullptr && !h->closure_on && !h->link_table;
+}
 
 // The kernel the next step with these arguments runs.  The cell-pair kernel moves 8-byte
 // (float32) or 4-byte (Float16C) words, so it needs 8-byte aligned population buffers; others
@@ -186,6 +208,7 @@ bool use_pair(const lbm_handle* h) { return h->path == 3 && h->step_pair != null
 StepLaunch step_fn(const lbm_handle* h, const StepArgs& a) {
     if (!use_tile(h)) return h->step;
     if (h->closure_on) return h->step_learned;
+    if (h->link_table) return h->step_links;
     if (use_pair(h) && ((reinterpret_cast<uintptr_t>(a.f_in) | reinterpret_cast<uintptr_t>(a.f_out)) & 7u) == 0u)
         return h->step_pair;
     return h->step_tile;
@@ -344,6 +367,10 @@ lbm_status lbm_create(const lbm_config_t* cfg, const lbm_grid_t* grid, lbm_handl
                  : grid->lattice == LBM_D2Q9 ? get_pair_step_d2q9(f16, co, les, fast)
                  : grid->lattice == LBM_D3Q19 ? get_pair_step_d3q19(f16, co, les, fast)
                                               : get_pair_step_d3q27(f16, co, les, fast);
+    h->step_links = !(tile_ok && m == LBM_DOUBLE_BUFFER) ? nullptr
+                  : grid->lattice == LBM_D2Q9 ? get_links_tile_step_d2q9(f16, co, les, fast)
+                  : grid->lattice == LBM_D3Q19 ? get_links_tile_step_d3q19(f16, co, les, fast)
+                                               : get_links_tile_step_d3q27(f16, co, les, fast);
     h->path = 0;
     h->ntiles = h->lay.ncells / h->lay.T;
     h->mx = (uint32_t)grid->tx - 1u;
@@ -363,6 +390,13 @@ lbm_status lbm_create(const lbm_config_t* cfg, const lbm_grid_t* grid, lbm_handl
     std::memset(&h->closure_uniform, 0, sizeof(h->closure_uniform));
     h->closure_on = 0;
     h->capture_stream = nullptr;
+    h->link_table = nullptr;
+    h->link_dist = nullptr;
+    h->link_id = nullptr;
+    h->link_force = nullptr;
+    h->n_links = 0;
+    h->q_clamp = 0.f;
+    h->bouzidi = 0;
     cudaError_t e = cudaGetDevice(&h->device);
     if (e == cudaSuccess) e = cudaDeviceGetAttribute(&h->sm_count, cudaDevAttrMultiProcessorCount, h->device);
     if (e == cudaSuccess) e = cudaMalloc(&h->scratch, sizeof(double) * (kReduceBlocks * kReduceWidth + 8));
@@ -391,8 +425,63 @@ lbm_status lbm_destroy(lbm_handle* h) {
     if (h->changed) cudaFree(h->changed);
     if (h->tile_near) cudaFree(h->tile_near);
     if (h->closure) cudaFree(h->closure);
+    if (h->link_table) cudaFree(h->link_table);
+    if (h->link_dist) cudaFree(h->link_dist);
+    if (h->link_id) cudaFree(h->link_id);
     if (h->capture_stream) cudaStreamDestroy(h->capture_stream);
     delete h;
+    return LBM_OK;
+}
+
+lbm_status lbm_set_links(lbm_handle* h, const int32_t* fluid_ids, const int32_t* dirs, const float* dists,
+                         int64_t n_links, int32_t method, float q_clamp, float* link_force, void* stream) {
+    if (check_handle(h)) return LBM_EINVAL;
+    if (n_links < 0 || n_links >= ((int64_t)1 << 31)) return fail(LBM_EINVAL, "n_links must be in [0, 2^31)");
+    if (n_links > 0 && h->cfg.lbm_method != LBM_DOUBLE_BUFFER)
+        return fail(LBM_EUNSUPPORTED, "interpolated bounce-back needs the double-buffer method");
+    if (method != LBM_BB_MID_GRID && method != LBM_BB_BOUZIDI) return fail(LBM_EINVAL, "unknown bounce-back method");
+    if (n_links > 0 && (!h->step_links || h->path == 1))
+        return fail(LBM_EUNSUPPORTED, "links fused into the step need the block-per-tile kernel: 256-cell "
+                                      "power-of-two tiles, Q*N < 2^31, kernel path not forced to generic");
+    if (n_links > 0 && h->closure_on)
+        return fail(LBM_EUNSUPPORTED, "links fused into the step and the learned closure are not built together");
+    if (n_links > 0 && (!fluid_ids || !dirs || !dists)) return fail(LBM_EINVAL, "null link array");
+    cudaStream_t s = (cudaStream_t)stream;
+    LinkTables lt;
+    if (n_links > 0) {
+        std::vector<int32_t> ids(n_links), dv(n_links);
+        std::vector<float> qv(n_links);
+        LBM_CK(cudaMemcpyAsync(ids.data(), fluid_ids, sizeof(int32_t) * n_links, cudaMemcpyDeviceToHost, s));
+        LBM_CK(cudaMemcpyAsync(dv.data(), dirs, sizeof(int32_t) * n_links, cudaMemcpyDeviceToHost, s));
+        LBM_CK(cudaMemcpyAsync(qv.data(), dists, sizeof(float) * n_links, cudaMemcpyDeviceToHost, s));
+        LBM_CK(cudaStreamSynchronize(s));
+        const std::string err = build_link_tables(h->lay.ncells, lattice_q(h->grid.lattice), n_links, nullptr, nullptr,
+                                                  nullptr, 1, ids.data(), dv.data(), qv.data(), lt);
+        if (!err.empty()) return fail(LBM_EINVAL, "lbm_set_links: " + err);
+    }
+    // steps in flight may read the current tables; cached graphs hold the old arguments
+    LBM_CK(cudaDeviceSynchronize());
+    for (auto& kv : h->graphs) cudaGraphExecDestroy(kv.second);
+    h->graphs.clear();
+    if (h->link_table) cudaFree(h->link_table);
+    if (h->link_dist) cudaFree(h->link_dist);
+    if (h->link_id) cudaFree(h->link_id);
+    h->link_table = nullptr;
+    h->link_dist = nullptr;
+    h->link_id = nullptr;
+    h->link_force = nullptr;
+    h->n_links = 0;
+    if (n_links == 0) return LBM_OK;
+    LBM_CK(cudaMalloc(&h->link_table, sizeof(uint2) * lt.table.size()));
+    LBM_CK(cudaMalloc(&h->link_dist, sizeof(float) * n_links));
+    LBM_CK(cudaMalloc(&h->link_id, sizeof(int32_t) * n_links));
+    LBM_CK(cudaMemcpy(h->link_table, lt.table.data(), sizeof(uint2) * lt.table.size(), cudaMemcpyHostToDevice));
+    LBM_CK(cudaMemcpy(h->link_dist, lt.dist.data(), sizeof(float) * n_links, cudaMemcpyHostToDevice));
+    LBM_CK(cudaMemcpy(h->link_id, lt.id.data(), sizeof(int32_t) * n_links, cudaMemcpyHostToDevice));
+    h->link_force = link_force;
+    h->n_links = n_links;
+    h->q_clamp = q_clamp;
+    h->bouzidi = method == LBM_BB_BOUZIDI;
     return LBM_OK;
 }
 
@@ -400,6 +489,8 @@ lbm_status lbm_set_closure(lbm_handle* h, const lbm_closure_t* closure) {
     if (check_handle(h)) return LBM_EINVAL;
     if (closure && !h->cfg.LES)
         return fail(LBM_EUNSUPPORTED, "the learned closure replaces Smagorinsky: the configuration needs LES");
+    if (closure && h->link_table)
+        return fail(LBM_EUNSUPPORTED, "links fused into the step and the learned closure are not built together");
     if (closure && (!h->step_learned || h->path == 1))
         return fail(LBM_EUNSUPPORTED, "the learned closure runs in the block-per-tile kernel: 256-cell "
                                       "power-of-two tiles, Q*N < 2^31, kernel path not forced to generic");
@@ -445,6 +536,8 @@ lbm_status lbm_set_kernel_path(lbm_handle* h, int32_t path) {
                                       "tiles with tx >= 2 and Q*N < 2^31");
     if (path == 1 && h->closure_on)
         return fail(LBM_EUNSUPPORTED, "the learned closure runs in the block-per-tile kernel only");
+    if (path == 1 && h->link_table)
+        return fail(LBM_EUNSUPPORTED, "links fused into the step (lbm_set_links) run in the block-per-tile kernel only");
     h->path = path;
     return LBM_OK;
 }

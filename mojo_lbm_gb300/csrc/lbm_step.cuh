@@ -38,6 +38,17 @@ struct StepArgs {
                                // holds a flag other than plain FLUID (warp_near)
     const uint2* cell_masks;   // per cell of such a warp: (raw_solid, nib_solid), cell_solid_masks
     uint32_t mx, my, shx, shxy; // lx = t & mx, ly = (t >> shx) & my, lz = t >> shxy
+    // interpolated bounce-back fused into the step (block-per-tile kernels, double buffer): per
+    // cell, (bit i set for each link whose wall node is x + c_i, index of its first link in the
+    // links' order: by cell, then by direction); per link in that order its wall distance and its
+    // index in the caller's arrays (for link_force, link_stride floats per component)
+    const uint2* link_table;   // null: no fused links
+    const float* link_dist;
+    const int32_t* link_id;
+    float* link_force;         // or null
+    int64_t link_stride;
+    float q_clamp;
+    int32_t bouzidi;
 };
 
 // Storage traits: float32, or Float16C codes decoded to float32 (load_f / store_f,
@@ -823,13 +834,74 @@ __device__ __forceinline__ void tile_cell_masks(const StepArgs& a, uint32_t tile
     masks[n] = cell_solid_masks<L>(a.flags, n, dc);
 }
 
+// Interpolated bounce-back fused into the step: the node-wise form of the reference's WIP kernel
+// (src/lbm/geometry/nodewise_interpolated_BB.mojo:46-185) with the interpolation of its working
+// link-wise kernel (geometry/interpolated_BB.mojo:102-141), so that the fused step reproduces the
+// link-wise path (step, then linkwise_bounceback_kernel on the lattice it wrote).  For each link
+// (x, i) of this cell, i pointing into the wall, the mid-grid bounce-back has just put
+// f_in(x, i) into f[j], j = opp(i); with q = max(distance, q_clamp) it becomes Bouzidi's
+//   q > 1/2:  f_in(x, i) / (2q) + (2q - 1) / (2q) f_in(x, j)
+//   q <= 1/2: 2q f_in(x, i) + (1 - 2q) f_in(x - c_i, j)
+// which is the value the link-wise kernel stores in (x, i) for the next step's bounce-back to read;
+// the force c_i (f_in(x, i) + f_bb) (+ 2 w_i under DDF shift, output/drag.mojo:88-93) is the link's
+// at the step that wrote f_in.  A link whose wall node is not a raw SOLID flag changes nothing here;
+// the link-wise path's value in (x, i) is then read by no step either (the wall node is skipped as
+// SOLID or pulls its own slot).  The reference's WIP kernel also shifts the interpolation's mass
+// change into f_0 (:170,178); the link-wise path does not, nor does this.  SCALED: f holds
+// populations times 2^-112, and so do the loaded values.  dp: the cell's element deltas.
+template <class L, bool SCALED, class S, class Ld>
+__device__ __forceinline__ void fused_links(float (&f)[L::Q], const uint2 lt, const uint32_t raw_solid,
+                                            const StepArgs& a, const S* fin, const int32_t own,
+                                            const int32_t (&dp)[3][3], Ld&& ld) {
+    constexpr int Q = L::Q, D = L::D;
+    constexpr uint32_t T = kTileCells;
+    uint32_t k = lt.y;
+    static_for<1, Q>([&](auto qc) {
+        constexpr int i = qc.value, j = opp<L>(i);
+        if ((lt.x >> i) & 1u) {
+            if ((raw_solid >> j) & 1u) {
+                float qd = __ldg(a.link_dist + k);
+                qd = qd < a.q_clamp ? a.q_clamp : qd;
+                const float f_into = f[j];
+                float f_bb = f_into;
+                if (a.bouzidi) {
+                    if (qd > 0.5f) {
+                        const float f_out = ld(fin + own + (int32_t)(T * j));
+                        f_bb = 0.5f / qd * f_into + (2.f * qd - 1.f) / (2.f * qd) * f_out;
+                    } else {
+                        constexpr int sx = L::c(j, 0), sy = L::c(j, 1), sz = L::c(j, 2);  // x - c_i = x + c_j
+                        const int32_t o = own + dp[0][sx + 1] + dp[1][sy + 1] + dp[2][sz + 1];
+                        const float f_xff = ld(fin + o + (int32_t)(T * j));
+                        f_bb = 2.f * qd * f_into + (1.f - 2.f * qd) * f_xff;
+                    }
+                    f[j] = f_bb;
+                }
+                if (a.link_force) {
+                    constexpr float w = wf<L>(i);
+                    float fa = f_into, fb = f_bb;
+                    if constexpr (SCALED) { fa *= 0x1p112f; fb *= 0x1p112f; }
+                    if (a.ddf) { fa += w; fb += w; }
+                    const int64_t id = __ldg(a.link_id + k);
+                    static_for<0, D>([&](auto dc) {
+                        constexpr int cd = L::c(i, dc.value);
+                        a.link_force[id + a.link_stride * dc.value] = (float)cd * (fa + fb);
+                    });
+                }
+            }
+            ++k;
+        }
+    });
+}
+
 // The per-thread body of the block-per-tile step: thread `tid` of the CTA that owns tile `tile`.
 // Every lane of a warp must call it (the learned closure `cl`, staged in shared memory, is
 // evaluated by whole warps).  Learned closure: fbuf is this warp's
 // population stash ((Q+3)/4 x 32 float4 of shared memory).
 // FAST: the fast-arithmetic collision (collide_fast, lbm_fast.cuh), with scaled Float16C codes
-// when the collision is linear in f.
-template <class L, int METHOD, bool F16C, int COLL, int LES, bool FAST = false>
+// when the collision is linear in f.  LINKS: the interpolated bounce-back of the links in
+// a.link_table fused into the stream (fused_links; double buffer).  It is a separate build because
+// its code would raise the register demand of every kernel beyond the budget of 5 CTAs per SM.
+template <class L, int METHOD, bool F16C, int COLL, int LES, bool FAST = false, bool LINKS = false>
 __device__ __forceinline__ void tile_step(const StepArgs& a, const uint32_t tile, const uint32_t tid,
                                           const ClosureDev* cl = nullptr, float4* fbuf = nullptr,
                                           int32_t near = -1) {
@@ -839,6 +911,7 @@ __device__ __forceinline__ void tile_step(const StepArgs& a, const uint32_t tile
     constexpr uint32_t T = kTileCells;
     constexpr bool ESO = METHOD == LBM_ESOTERIC_PULL;
     static_assert(!(FAST && LES == kLesLearned), "the learned closure has its own tolerance build");
+    static_assert(!(LINKS && ESO), "the fused links are double-buffer only");
     constexpr bool SCALED = FAST && F16C && !LES && COLL != LBM_KBC;
     auto ld = [](const S* p) -> float {
         if constexpr (SCALED) return P::ld_scaled(p);
@@ -927,6 +1000,12 @@ __device__ __forceinline__ void tile_step(const StepArgs& a, const uint32_t tile
                     constexpr int q = qc.value;
                     if ((raw_solid >> q) & 1u) f[q] = ld(fin + own + (int32_t)(T * opp<L>(q)));
                 });
+            if constexpr (LINKS) {
+                if (raw_solid) {
+                    const uint2 lt = __ldg(a.link_table + n);
+                    if (lt.x) fused_links<L, SCALED>(f, lt, raw_solid, a, fin, own, dp, ld);
+                }
+            }
         }
         if (a.moving && nib_solid) {
             moving_wall<L, SCALED>(f, nib_solid, a.bc, T, [&](auto qc) -> uint64_t {
@@ -978,11 +1057,21 @@ __device__ __forceinline__ void tile_step(const StepArgs& a, const uint32_t tile
 #define LBM_TILE_MIN_BLOCKS_HEAVY 3
 #endif
 
-template <class L, int METHOD, bool F16C, int COLL, int LES, bool FAST = false>
-__global__ void __launch_bounds__(256, (L::Q == 9) ? 5 : ((COLL == LBM_KBC || L::Q == 27) ? LBM_TILE_MIN_BLOCKS_HEAVY : LBM_TILE_MIN_BLOCKS))
+// Resident CTAs per SM the block-per-tile kernels are built for: D2Q9 5, the KBC and D3Q27 kernels
+// LBM_TILE_MIN_BLOCKS_HEAVY, the others LBM_TILE_MIN_BLOCKS (5: 48 registers); the fused-link
+// kernels 4 (their interpolation needs 64 registers to run without spilling).
+template <class L, int COLL, bool LINKS>
+constexpr int tile_min_blocks() {
+    constexpr bool heavy = COLL == LBM_KBC || L::Q == 27;
+    if constexpr (LINKS) return heavy ? LBM_TILE_MIN_BLOCKS_HEAVY : 4;
+    else return (L::Q == 9) ? 5 : (heavy ? LBM_TILE_MIN_BLOCKS_HEAVY : LBM_TILE_MIN_BLOCKS);
+}
+
+template <class L, int METHOD, bool F16C, int COLL, int LES, bool FAST = false, bool LINKS = false>
+__global__ void __launch_bounds__(256, (tile_min_blocks<L, COLL, LINKS>()))
     step_kernel_tile(const StepArgs a) {
     static_assert(LES != kLesLearned, "the learned closure runs in step_kernel_learned");
-    tile_step<L, METHOD, F16C, COLL, LES, FAST>(a, blockIdx.x, threadIdx.x);
+    tile_step<L, METHOD, F16C, COLL, LES, FAST, LINKS>(a, blockIdx.x, threadIdx.x);
 }
 
 #ifndef LBM_LEARNED_MIN_BLOCKS
@@ -1036,6 +1125,18 @@ cudaError_t launch_step_tile(const StepArgs& a, int, cudaStream_t s) {
 template <class L, int METHOD, bool F16C, int COLL, int LES>
 cudaError_t launch_step_tile_fast(const StepArgs& a, int, cudaStream_t s) {
     step_kernel_tile<L, METHOD, F16C, COLL, LES, true><<<a.lay.ncells / kTileCells, kTileCells, 0, s>>>(a);
+    return cudaGetLastError();
+}
+
+// The block-per-tile kernel with fused links (lbm_set_links), exact and fast arithmetic.
+template <class L, int METHOD, bool F16C, int COLL, int LES>
+cudaError_t launch_step_tile_links(const StepArgs& a, int, cudaStream_t s) {
+    step_kernel_tile<L, METHOD, F16C, COLL, LES, false, true><<<a.lay.ncells / kTileCells, kTileCells, 0, s>>>(a);
+    return cudaGetLastError();
+}
+template <class L, int METHOD, bool F16C, int COLL, int LES>
+cudaError_t launch_step_tile_links_fast(const StepArgs& a, int, cudaStream_t s) {
+    step_kernel_tile<L, METHOD, F16C, COLL, LES, true, true><<<a.lay.ncells / kTileCells, kTileCells, 0, s>>>(a);
     return cudaGetLastError();
 }
 

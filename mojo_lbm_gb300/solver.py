@@ -113,6 +113,15 @@ class Solver:
                                                 ptr(dists), n, int(method), int(bool(compute_force)),
                                                 float(q_clamp), stream_ptr(stream)))
 
+    def set_links(self, fluid_ids, dirs, dists, method: int, q_clamp: float = 0.0, link_force=None,
+                  stream=None) -> None:
+        """Registers links whose interpolated bounce-back every following double-buffer step applies
+        inside the step kernel (lbm_set_links; the node-wise form of
+        src/lbm/geometry/nodewise_interpolated_BB.mojo:46-185).  fluid_ids = None removes them."""
+        n = 0 if fluid_ids is None else (int(fluid_ids.numel()) if hasattr(fluid_ids, "numel") else len(fluid_ids))
+        check(self._lib.lbm_set_links(self._h, ptr(fluid_ids), ptr(dirs), ptr(dists), n, int(method),
+                                      float(q_clamp), ptr(link_force), stream_ptr(stream)))
+
     def sum_link_force(self, link_force, n_links: int, stream=None) -> tuple[float, ...]:
         out = (C.c_double * 3)()
         check(self._lib.lbm_sum_link_force(self._h, ptr(link_force), int(n_links), out, stream_ptr(stream)))
