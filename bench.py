@@ -513,6 +513,8 @@ def run_batch(args, wl: dict):
     dom, ids, dirs, dists, method = links_of(chans, dev)
     force = torch.zeros(ids.numel() * 2, device=dev)
     batch.set_links(dom, ids, dirs, dists, method, 0.0, force)
+    links_mode = args.links or wl.get("links", "separate")
+    batch.set_link_mode(links_mode == "fused")
     N = batch.num_cells
     stream = torch.cuda.current_stream(dev)
     batch.run(args.warmup, 0, stream)
@@ -524,7 +526,7 @@ def run_batch(args, wl: dict):
     clk = clocks.stop() if clocks else None
     t_ms, units = aggregate(statistics.median(reps), float(N) * K, world, dev)
     mlups = units / (t_ms * 1e-3) / 1e6
-    launch_ms = t_ms / K  # one persistent step launch + one link launch per step, averaged
+    launch_ms = t_ms / K  # per step: the persistent step launch (+ the link launch when separate), averaged
 
     # end to end through the public API: every domain's f, bc and flags uploaded from pinned host
     # memory, K batched steps, every f downloaded, inside the timed region
@@ -564,6 +566,8 @@ def run_batch(args, wl: dict):
         "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded channels from rest)",
         "config": {"workload": wl["desc"], "domains": len(chans), "cells": N, "links": int(ids.numel()),
                    "tile": list(wl["tile"]), "tile_source": tile_source,
+                   "link_mode": "fused into the step kernel" if links_mode == "fused"
+                            else "link-wise kernel after every step",
                    "timing": f"CUDA events around each of {len(reps)} replays of the K-step graph on the launching "
                              f"stream (at least {args.repeat_seconds:g} s in all); value from the median replay",
                    "repeats": len(reps),
@@ -571,7 +575,7 @@ def run_batch(args, wl: dict):
         "roofline": {"bound": "hbm", "achieved": round(achieved, 1), "peak": peak, "unit": "GB/s",
                      "frac": round(achieved / peak, 4), "traffic": traffic,
                      "note": f"72 B/update x {N} cells / average per-step time over the timed region {launch_ms:.4f} "
-                             f"ms (persistent step + link kernel); peak {peak_kind}; traffic = ncu dram bytes per "
+                             f"ms (persistent step{'' if links_mode == 'fused' else ' + link kernel'}); peak {peak_kind}; traffic = ncu dram bytes per "
                              f"launch ({traffic_src or 'no capture committed'}, scaled by cells)"},
         "cpu_baseline": None,
         "e2e": {"value": round(e2e_units / (e2e_ms * 1e-3) / 1e6, 2), "unit": "MLUPs",
@@ -580,7 +584,7 @@ def run_batch(args, wl: dict):
                         f"every f downloaded inside the timed region, amortised over the {K} steps (after one "
                         "untimed pass of 64 steps); the domains' arrays are slices of one allocation per kind, "
                         "so each transfer is one copy"},
-        "gpu_launches": 2 * K + 3, "clocks": clk,
+        "gpu_launches": (K if links_mode == "fused" else 2 * K) + 3, "clocks": clk,
     }
     print(json.dumps(line), flush=True)
     return line
@@ -699,6 +703,9 @@ def main(argv=None):
     ap.add_argument("--kernel", choices=["auto", "generic", "tile", "pair"], default=None,
                     help="step kernel: generic, block-per-tile, or cell-pair block-per-tile (two cells per thread "
                          "along x; double buffer); default per workload")
+    ap.add_argument("--links", choices=["separate", "fused"], default=None,
+                    help="batched workload: Bouzidi links by the link-wise kernel after every step, or fused into "
+                         "the step kernel; default per workload")
     ap.add_argument("--repeat-seconds", type=float, default=2.0,
                     help="replay the timed K steps until this much timed work has passed (median replay reported)")
     ap.add_argument("--no-cpu-baseline", action="store_true")

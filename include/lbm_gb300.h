@@ -293,6 +293,15 @@ lbm_status lbm_batch_set_links(lbm_batch* b, const int32_t* domain, const int32_
                                const int32_t* dirs, const float* dists, int64_t n_links,
                                int32_t method, float q_clamp, float* link_force);
 
+/* How lbm_batch_run applies the links of lbm_batch_set_links: LBM_LINKS_SEPARATE (default) runs the
+ * link-wise kernel over all links after every batched step; LBM_LINKS_FUSED applies them inside the
+ * batched step kernel as lbm_set_links does for one domain (one kernel per step; the link slots hold
+ * the step's own values and the forces lag one step, as described there).  The fused tables are
+ * built from the link arrays at the next lbm_batch_run (the arrays must still hold the links then).
+ * Double buffer only (LBM_EUNSUPPORTED otherwise). */
+enum { LBM_LINKS_SEPARATE = 0, LBM_LINKS_FUSED = 1 };
+lbm_status lbm_batch_set_link_mode(lbm_batch* b, int32_t mode);
+
 /* n_steps steps of every domain, replayed from a CUDA graph of 64 steps. */
 lbm_status lbm_batch_run(lbm_batch* b, int64_t n_steps, int64_t first_step, void* stream);
 

@@ -12,6 +12,7 @@ from pathlib import Path
 LIB_PATH = Path(__file__).resolve().parent / "liblbm_gb300.so"
 
 LBM_OK, LBM_EINVAL, LBM_ECUDA, LBM_ENAN, LBM_ETIMEOUT, LBM_ENOMEM, LBM_EUNSUPPORTED = range(7)
+LBM_LINKS_SEPARATE, LBM_LINKS_FUSED = 0, 1
 STATUS_NAMES = {0: "LBM_OK", 1: "LBM_EINVAL", 2: "LBM_ECUDA", 3: "LBM_ENAN", 4: "LBM_ETIMEOUT",
                 5: "LBM_ENOMEM", 6: "LBM_EUNSUPPORTED"}
 
@@ -86,6 +87,7 @@ SIGNATURES = {
     "lbm_batch_destroy": (_i32, [_vp]),
     "lbm_batch_set_domain": (_i32, [_vp, _i32, _vp, _vp, _vp, _vp, _f32]),
     "lbm_batch_set_links": (_i32, [_vp, _vp, _vp, _vp, _vp, _i64, _i32, _f32, _vp]),
+    "lbm_batch_set_link_mode": (_i32, [_vp, _i32]),
     "lbm_batch_run": (_i32, [_vp, _i64, _i64, _vp]),
     "lbm_batch_cells": (_i64, [_vp]),
     "lbm_set_closure": (_i32, [_vp, C.POINTER(lbm_closure_t)]),

@@ -48,5 +48,10 @@ class BatchSolver:
         check(self._lib.lbm_batch_set_links(self._h, ptr(domain), ptr(fluid_ids), ptr(dirs), ptr(dists), n,
                                             int(method), float(q_clamp), ptr(link_force)))
 
+    def set_link_mode(self, fused: bool) -> None:
+        """True: the links are applied inside the batched step kernel (LBM_LINKS_FUSED, one kernel per
+        step); False: by the link-wise kernel after every step (LBM_LINKS_SEPARATE, the default)."""
+        check(self._lib.lbm_batch_set_link_mode(self._h, _capi.LBM_LINKS_FUSED if fused else _capi.LBM_LINKS_SEPARATE))
+
     def run(self, n_steps: int, first_step: int = 0, stream=None) -> None:
         check(self._lib.lbm_batch_run(self._h, int(n_steps), int(first_step), stream_ptr(stream)))

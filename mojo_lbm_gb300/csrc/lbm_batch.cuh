@@ -30,8 +30,16 @@ __device__ __forceinline__ uint32_t find_domain(const uint32_t* begin, uint32_t 
     return lo;
 }
 
-template <class L, int METHOD, bool F16C, int COLL, int LES>
-__global__ void __launch_bounds__(256, (L::Q == 9) ? 5 : ((COLL == LBM_KBC || L::Q == 27) ? 3 : 4)) step_kernel_batch(const BatchArgs b) {
+// Resident CTAs per SM of the batched kernel; LINKS: with the interpolated bounce-back fused in
+// (each descriptor's link table; tile_min_blocks of the single-domain kernel).
+template <class L, int COLL, bool LINKS>
+constexpr int batch_min_blocks() {
+    if constexpr (LINKS) return tile_min_blocks<L, COLL, true>();
+    else return (L::Q == 9) ? 5 : ((COLL == LBM_KBC || L::Q == 27) ? 3 : 4);
+}
+
+template <class L, int METHOD, bool F16C, int COLL, int LES, bool LINKS = false>
+__global__ void __launch_bounds__(256, (batch_min_blocks<L, COLL, LINKS>())) step_kernel_batch(const BatchArgs b) {
     __shared__ StepArgs sa;
     // a contiguous, equal share of the units per CTA: the domain changes rarely along it, so the
     // descriptor is reloaded only when it does
@@ -55,7 +63,7 @@ __global__ void __launch_bounds__(256, (L::Q == 9) ? 5 : ((COLL == LBM_KBC || L:
             __syncthreads();
             loaded = d;
         }
-        tile_step<L, METHOD, F16C, COLL, LES>(sa, u - __ldg(b.unit_begin + d), threadIdx.x);
+        tile_step<L, METHOD, F16C, COLL, LES, false, LINKS>(sa, u - __ldg(b.unit_begin + d), threadIdx.x);
     }
 }
 
@@ -119,20 +127,29 @@ __global__ void link_kernel_batch(const BatchLinkArgs b) {
 
 using BatchLaunch = cudaError_t (*)(const BatchArgs&, int sms, cudaStream_t);
 
-template <class L, int METHOD, bool F16C, int COLL, int LES>
-cudaError_t launch_step_batch(const BatchArgs& b, int sms, cudaStream_t s) {
+template <class L, int METHOD, bool F16C, int COLL, int LES, bool LINKS = false>
+cudaError_t launch_step_batch_impl(const BatchArgs& b, int sms, cudaStream_t s) {
     static int per_sm = 0;
     if (per_sm == 0) {
         const cudaError_t e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(
-            &per_sm, step_kernel_batch<L, METHOD, F16C, COLL, LES>, (int)kTileCells, 0);
+            &per_sm, step_kernel_batch<L, METHOD, F16C, COLL, LES, LINKS>, (int)kTileCells, 0);
         if (e != cudaSuccess) return e;
         if (per_sm < 1) per_sm = 1;
     }
     uint32_t grid = (uint32_t)(sms * per_sm);
     if (grid > b.total_units) grid = b.total_units;
     if (grid == 0) return cudaSuccess;
-    step_kernel_batch<L, METHOD, F16C, COLL, LES><<<grid, kTileCells, 0, s>>>(b);
+    step_kernel_batch<L, METHOD, F16C, COLL, LES, LINKS><<<grid, kTileCells, 0, s>>>(b);
     return cudaGetLastError();
+}
+template <class L, int METHOD, bool F16C, int COLL, int LES>
+cudaError_t launch_step_batch(const BatchArgs& b, int sms, cudaStream_t s) {
+    return launch_step_batch_impl<L, METHOD, F16C, COLL, LES, false>(b, sms, s);
+}
+// The batched step with the links fused in (lbm_batch_set_link_mode, double buffer).
+template <class L, int METHOD, bool F16C, int COLL, int LES>
+cudaError_t launch_step_batch_links(const BatchArgs& b, int sms, cudaStream_t s) {
+    return launch_step_batch_impl<L, METHOD, F16C, COLL, LES, true>(b, sms, s);
 }
 
 }  // namespace lbm

@@ -9,12 +9,16 @@
 #include <vector>
 
 #include "lbm_batch.cuh"
+#include "lbm_link_tables.h"
 
 namespace lbm {
 void set_last_error(const char* msg);  // lbm_capi.cu
 BatchLaunch get_batch_step_d2q9(int, int, int, int);
 BatchLaunch get_batch_step_d3q19(int, int, int, int);
 BatchLaunch get_batch_step_d3q27(int, int, int, int);
+BatchLaunch get_batch_links_step_d2q9(int, int, int);
+BatchLaunch get_batch_links_step_d3q19(int, int, int);
+BatchLaunch get_batch_links_step_d3q27(int, int, int);
 cudaError_t launch_link_batch_d2q9(const BatchLinkArgs&, bool, cudaStream_t);
 cudaError_t launch_link_batch_d3q19(const BatchLinkArgs&, bool, cudaStream_t);
 cudaError_t launch_link_batch_d3q27(const BatchLinkArgs&, bool, cudaStream_t);
@@ -45,6 +49,7 @@ struct lbm_batch {
     bool summary_valid = false;
     bool dirty = true;
     BatchLaunch step = nullptr;
+    BatchLaunch step_links = nullptr;  // the step with the links fused in (double buffer), or null
     // links (caller-owned device arrays, concatenated over domains)
     const int32_t *l_dom = nullptr, *l_ids = nullptr, *l_dirs = nullptr;
     const float* l_dists = nullptr;
@@ -52,6 +57,11 @@ struct lbm_batch {
     int64_t n_links = 0;
     int32_t l_method = LBM_BB_BOUZIDI;
     float l_qclamp = 0.f;
+    int32_t link_mode = LBM_LINKS_SEPARATE;
+    bool tables_stale = true;          // the fused tables do not hold the current links
+    uint2* d_link_table = nullptr;     // fused: per cell of the batch (256 cells per unit)
+    float* d_link_dist = nullptr;
+    int32_t* d_link_id = nullptr;
     int sms = 1;
     cudaStream_t capture_stream = nullptr;
     std::map<int, cudaGraphExec_t> graphs;  // keyed by the parity of the first step
@@ -128,15 +138,76 @@ lbm_status launch_links(lbm_batch* b, const StepArgs* dom, cudaStream_t s) {
     return LBM_OK;
 }
 
-// One step of every domain: the persistent step kernel, then the link-wise bounce-back.
+bool fused_links(const lbm_batch* b) { return b->link_mode == LBM_LINKS_FUSED && b->n_links > 0; }
+
+// One step of every domain: the persistent step kernel, then the link-wise bounce-back (or the
+// step kernel with the links fused in).
 lbm_status batch_step(lbm_batch* b, bool parity_odd, cudaStream_t s) {
     BatchArgs a;
     a.dom = parity_odd ? b->d_odd : b->d_even;
     a.unit_begin = b->d_begin;
     a.ndom = (uint32_t)b->ndom;
     a.total_units = b->unit_begin.back();
+    if (fused_links(b)) {
+        LBM_BCK(b->step_links(a, b->sms, s));
+        return LBM_OK;
+    }
     LBM_BCK(b->step(a, b->sms, s));
     return launch_links(b, a.dom, s);
+}
+
+void free_tables(lbm_batch* b) {
+    cudaFree(b->d_link_table);
+    cudaFree(b->d_link_dist);
+    cudaFree(b->d_link_id);
+    b->d_link_table = nullptr;
+    b->d_link_dist = nullptr;
+    b->d_link_id = nullptr;
+}
+
+// The fused mode's per-cell link table from the caller's link arrays (the batch's cells numbered
+// unit after unit, 256 per unit), and the descriptors' pointers into it.
+lbm_status build_tables(lbm_batch* b, cudaStream_t s) {
+    const int64_t n = b->n_links;
+    const uint64_t cells = (uint64_t)b->unit_begin.back() * kTileCells;
+    std::vector<int32_t> dom(n), ids(n), dirs(n);
+    std::vector<float> dists(n);
+    LBM_BCK(cudaMemcpyAsync(dom.data(), b->l_dom, sizeof(int32_t) * n, cudaMemcpyDeviceToHost, s));
+    LBM_BCK(cudaMemcpyAsync(ids.data(), b->l_ids, sizeof(int32_t) * n, cudaMemcpyDeviceToHost, s));
+    LBM_BCK(cudaMemcpyAsync(dirs.data(), b->l_dirs, sizeof(int32_t) * n, cudaMemcpyDeviceToHost, s));
+    LBM_BCK(cudaMemcpyAsync(dists.data(), b->l_dists, sizeof(float) * n, cudaMemcpyDeviceToHost, s));
+    LBM_BCK(cudaStreamSynchronize(s));
+    std::vector<uint64_t> cell0(b->ndom), ncells(b->ndom);
+    for (int32_t d = 0; d < b->ndom; ++d) {
+        cell0[d] = (uint64_t)b->unit_begin[d] * kTileCells;
+        ncells[d] = (uint64_t)(b->unit_begin[d + 1] - b->unit_begin[d]) * kTileCells;
+    }
+    LinkTables lt;
+    const int Q = b->lattice == LBM_D2Q9 ? 9 : b->lattice == LBM_D3Q19 ? 19 : 27;
+    const std::string err = build_link_tables((int64_t)cells, Q, n, dom.data(), cell0.data(), ncells.data(), b->ndom,
+                                              ids.data(), dirs.data(), dists.data(), lt);
+    if (!err.empty()) return bfail(LBM_EINVAL, "lbm_batch_run (fused links): " + err);
+    free_tables(b);
+    LBM_BCK(cudaMalloc(&b->d_link_table, sizeof(uint2) * lt.table.size()));
+    LBM_BCK(cudaMalloc(&b->d_link_dist, sizeof(float) * n));
+    LBM_BCK(cudaMalloc(&b->d_link_id, sizeof(int32_t) * n));
+    LBM_BCK(cudaMemcpy(b->d_link_table, lt.table.data(), sizeof(uint2) * lt.table.size(), cudaMemcpyHostToDevice));
+    LBM_BCK(cudaMemcpy(b->d_link_dist, lt.dist.data(), sizeof(float) * n, cudaMemcpyHostToDevice));
+    LBM_BCK(cudaMemcpy(b->d_link_id, lt.id.data(), sizeof(int32_t) * n, cudaMemcpyHostToDevice));
+    for (int32_t d = 0; d < b->ndom; ++d) {
+        for (StepArgs* a : {&b->even[d], &b->odd[d]}) {
+            a->link_table = b->d_link_table + cell0[d];
+            a->link_dist = b->d_link_dist;
+            a->link_id = b->d_link_id;
+            a->link_force = b->l_force;
+            a->link_stride = n;
+            a->q_clamp = b->l_qclamp;
+            a->bouzidi = b->l_method == LBM_BB_BOUZIDI;
+        }
+    }
+    b->tables_stale = false;
+    b->dirty = true;
+    return LBM_OK;
 }
 
 }  // namespace
@@ -182,6 +253,10 @@ lbm_status lbm_batch_create(const lbm_config_t* cfg, int32_t n_domains, const lb
     b->step = lat == LBM_D2Q9 ? get_batch_step_d2q9(m, f16, co, les)
             : lat == LBM_D3Q19 ? get_batch_step_d3q19(m, f16, co, les)
                                : get_batch_step_d3q27(m, f16, co, les);
+    b->step_links = m != LBM_DOUBLE_BUFFER ? nullptr
+                  : lat == LBM_D2Q9 ? get_batch_links_step_d2q9(f16, co, les)
+                  : lat == LBM_D3Q19 ? get_batch_links_step_d3q19(f16, co, les)
+                                     : get_batch_links_step_d3q27(f16, co, les);
     int dev = 0;
     cudaError_t e = cudaGetDevice(&dev);
     if (e == cudaSuccess) e = cudaDeviceGetAttribute(&b->sms, cudaDevAttrMultiProcessorCount, dev);
@@ -216,6 +291,7 @@ lbm_status lbm_batch_destroy(lbm_batch* b) {
     cudaFree(b->d_flags_seen);
     cudaFree(b->d_cell_masks);
     cudaFree(b->d_changed);
+    free_tables(b);
     if (b->capture_stream) cudaStreamDestroy(b->capture_stream);
     delete b;
     return LBM_OK;
@@ -272,6 +348,7 @@ lbm_status lbm_batch_set_domain(lbm_batch* b, int32_t i, void* f_a, void* f_b, f
     }
     b->even[i] = ev;
     b->odd[i] = od;
+    b->tables_stale = true;  // the descriptors' link pointers are set when the tables are built
     b->set[i] = 1;
     b->dirty = true;
     return LBM_OK;
@@ -293,7 +370,22 @@ lbm_status lbm_batch_set_links(lbm_batch* b, const int32_t* domain, const int32_
     b->n_links = n_links;
     b->l_method = method;
     b->l_qclamp = q_clamp;
+    b->tables_stale = true;
     drop_graphs(b);
+    return LBM_OK;
+}
+
+lbm_status lbm_batch_set_link_mode(lbm_batch* b, int32_t mode) {
+    if (!b) return bfail(LBM_EINVAL, "null batch");
+    if (mode != LBM_LINKS_SEPARATE && mode != LBM_LINKS_FUSED)
+        return bfail(LBM_EINVAL, "link mode must be LBM_LINKS_SEPARATE or LBM_LINKS_FUSED");
+    if (mode == LBM_LINKS_FUSED && !b->step_links)
+        return bfail(LBM_EUNSUPPORTED, "fused links need the double-buffer method");
+    if (mode != b->link_mode) {
+        b->link_mode = mode;
+        b->tables_stale = true;
+        drop_graphs(b);
+    }
     return LBM_OK;
 }
 
@@ -304,6 +396,11 @@ lbm_status lbm_batch_run(lbm_batch* b, int64_t n_steps, int64_t first_step, void
         if (!b->set[i]) return bfail(LBM_EINVAL, "domain " + std::to_string(i) + " has no buffers");
     cudaStream_t s = (cudaStream_t)stream;
     if (n_steps == 0) return LBM_OK;
+    if (fused_links(b) && b->tables_stale) {
+        const lbm_status st = build_tables(b, s);
+        if (st != LBM_OK) return st;
+        drop_graphs(b);
+    }
     if (b->dirty) {
         LBM_BCK(cudaMemcpyAsync(b->d_even, b->even.data(), sizeof(StepArgs) * b->ndom, cudaMemcpyHostToDevice, s));
         LBM_BCK(cudaMemcpyAsync(b->d_odd, b->odd.data(), sizeof(StepArgs) * b->ndom, cudaMemcpyHostToDevice, s));

@@ -225,17 +225,29 @@ __device__ __forceinline__ void pair_step(const StepArgs& a, const uint32_t tile
     }
 }
 
+// Resident CTAs (of 128 threads) per SM the pair kernels are built for: the populations of two
+// cells stay in registers across both collisions, so the budget is wider than the per-cell
+// kernel's.  Float16C 8 (64 registers), float32 7 (72), TRT 6 (80), KBC and D3Q27 4 (128): the SRT
+// kernels run without spilling.
+#ifndef LBM_PAIR_MIN_BLOCKS_F16C
+#define LBM_PAIR_MIN_BLOCKS_F16C 8
+#endif
 #ifndef LBM_PAIR_MIN_BLOCKS
-#define LBM_PAIR_MIN_BLOCKS 6
+#define LBM_PAIR_MIN_BLOCKS 7
 #endif
 #ifndef LBM_PAIR_MIN_BLOCKS_HEAVY
 #define LBM_PAIR_MIN_BLOCKS_HEAVY 4
 #endif
+template <class L, bool F16C, int COLL>
+constexpr int pair_min_blocks() {
+    return (COLL == LBM_KBC || L::Q == 27) ? LBM_PAIR_MIN_BLOCKS_HEAVY
+           : COLL == LBM_TRT               ? 6
+           : F16C                          ? LBM_PAIR_MIN_BLOCKS_F16C
+                                           : LBM_PAIR_MIN_BLOCKS;
+}
 
 template <class L, bool F16C, int COLL, int LES, bool FAST>
-__global__ void __launch_bounds__(kPairThreads, (COLL == LBM_KBC || L::Q == 27) ? LBM_PAIR_MIN_BLOCKS_HEAVY
-                                                                                : LBM_PAIR_MIN_BLOCKS)
-    step_kernel_pair(const StepArgs a) {
+__global__ void __launch_bounds__(kPairThreads, (pair_min_blocks<L, F16C, COLL>())) step_kernel_pair(const StepArgs a) {
     static_assert(LES != kLesLearned, "the learned closure runs in step_kernel_learned");
     pair_step<L, F16C, COLL, LES, FAST>(a, blockIdx.x, threadIdx.x);
 }

@@ -170,3 +170,54 @@ def test_set_links_rejects_bad_links():
     s.set_links(None, None, None, Bounceback_method.BOUZIDI)  # removed: the generic kernel is allowed again
     s.set_kernel_path(1)
     s.close()
+
+
+def test_batch_fused_links_match_separate():
+    """Five cylinder channels of the batched workload: LBM_LINKS_FUSED (one kernel per step) against
+    LBM_LINKS_SEPARATE (the link-wise kernel after every step), word for word after a final link
+    pass, and the forces one step apart."""
+    import oracle as orc
+    from mojo_lbm_gb300.batch import BatchSolver
+    from mojo_lbm_gb300.workloads import cylinder_channels, links_of
+    chans = cylinder_channels(n=5, seed=3, nx_range=(96, 160), tile=(16, 16, 1))
+    dom, ids, dirs, dists, method = links_of(chans)
+    runs = {}
+    for fused in (False, True):
+        b = BatchSolver([c.grid for c in chans], chans[0].cfg)
+        bufs = []
+        for i, ch in enumerate(chans):
+            f = np.zeros(ch.grid.num_points * 9, np.float32)
+            orc.init(ch.cfg, ch.grid, 32, f)
+            fa, fb = _dev(f), _dev(f)
+            bct, flt = _dev(ch.bc), _dev(ch.flags)
+            if not fused:  # the link-wise path starts from a link pass over the initial state
+                s = Solver(ch.grid, ch.cfg)
+                sel = (dom == i).nonzero().flatten()
+                s.linkwise_bounceback(fa, None, ids[sel], dirs[sel], dists[sel], method, False, 0.0)
+                torch.cuda.synchronize()
+                s.close()
+            bufs.append((fa, fb, bct, flt))
+            b.set_domain(i, fa, fb, bct, flt, ch.tau)
+        force = torch.zeros(ids.numel() * 2, device="cuda")
+        b.set_links(dom, ids, dirs, dists, method, 0.0, force)
+        b.set_link_mode(fused)
+        b.run(STEPS - 1, 0)
+        f_prev = force.clone()
+        b.run(1, STEPS - 1)
+        torch.cuda.synchronize()
+        outs = []
+        for i, ch in enumerate(chans):
+            out = bufs[i][1] if STEPS % 2 == 1 else bufs[i][0]
+            if fused:
+                s = Solver(ch.grid, ch.cfg)
+                sel = (dom == i).nonzero().flatten()
+                s.linkwise_bounceback(out, None, ids[sel], dirs[sel], dists[sel], method, False, 0.0)
+                torch.cuda.synchronize()
+                s.close()
+            outs.append(out.cpu().numpy())
+        runs[fused] = (outs, f_prev.cpu().numpy(), force.cpu().numpy())
+        b.close()
+    (sep, sep_prev, _), (fus, _, fus_last) = runs[False], runs[True]
+    for a, c in zip(sep, fus):
+        assert np.array_equal(a.view(np.uint32), c.view(np.uint32))
+    assert np.array_equal(fus_last.view(np.uint32), sep_prev.view(np.uint32))
