@@ -227,10 +227,10 @@ __device__ __forceinline__ void pair_step(const StepArgs& a, const uint32_t tile
 
 // Resident CTAs (of 128 threads) per SM the pair kernels are built for: the populations of two
 // cells stay in registers across both collisions, so the budget is wider than the per-cell
-// kernel's.  Float16C 8 (64 registers), float32 7 (72), TRT 6 (80), KBC and D3Q27 4 (128): the SRT
-// kernels run without spilling.
+// kernel's.  Float16C and float32 7 (72 registers; measured against 6, 8 and 10 on the Float16C
+// cavity), TRT 6 (80), KBC and D3Q27 4 (128): the SRT kernels run without spilling.
 #ifndef LBM_PAIR_MIN_BLOCKS_F16C
-#define LBM_PAIR_MIN_BLOCKS_F16C 8
+#define LBM_PAIR_MIN_BLOCKS_F16C 7
 #endif
 #ifndef LBM_PAIR_MIN_BLOCKS
 #define LBM_PAIR_MIN_BLOCKS 7

@@ -1063,7 +1063,7 @@ __device__ __forceinline__ void tile_step(const StepArgs& a, const uint32_t tile
 template <class L, int COLL, bool LINKS>
 constexpr int tile_min_blocks() {
     constexpr bool heavy = COLL == LBM_KBC || L::Q == 27;
-    if constexpr (LINKS) return heavy ? LBM_TILE_MIN_BLOCKS_HEAVY : 4;
+    if constexpr (LINKS) return heavy ? LBM_TILE_MIN_BLOCKS_HEAVY : (L::Q == 9 ? 5 : 4);
     else return (L::Q == 9) ? 5 : (heavy ? LBM_TILE_MIN_BLOCKS_HEAVY : LBM_TILE_MIN_BLOCKS);
 }
 

@@ -8,8 +8,10 @@ over the initial state), so after K steps the two lattices differ only in the li
 one link-wise pass over the fused lattice closes that gap.  Float32 (exact arithmetic): every word
 equal, and the link forces the fused step k writes equal the link-wise forces of step k-1.
 Float16C: the link-wise path rounds the interpolated value to a 16-bit code before the next step
-reads it and the fused path does not, so values agree to the float32 tolerance plus two units in
-the code's last place (1e-6 + (2e-6 + 2^-9) |f|) after K steps.
+reads it and the fused path does not, so values agree to two units in the code's last place
+(2^-9 |f|) plus an absolute 8e-6 (two code units of a population of magnitude 0.01, the scale of
+the DDF-shifted populations, whose rounding difference the collision spreads to smaller
+neighbours) after K steps.
 """
 from __future__ import annotations
 
@@ -110,7 +112,7 @@ def _run_fused(grid, cfg, flags, bc, f0, body, method, tau, steps, by_run=False)
 def _close_f16(got, ref, what):
     g = oracle.f16c_decode(got).astype(np.float64)
     r = oracle.f16c_decode(ref).astype(np.float64)
-    tol = 1e-6 + (2e-6 + 2.0 ** -9) * np.abs(r)
+    tol = 8e-6 + 2.0 ** -9 * np.abs(r)
     bad = ~(np.abs(g - r) <= tol)
     assert not bad.any(), f"{what}: {int(bad.sum())} values beyond the tolerance (max |df| {np.abs(g - r).max():.3e})"
 
