@@ -41,8 +41,8 @@ typedef enum lbm_status {
     LBM_EINVAL = 1,       /* invalid argument or configuration                               */
     LBM_ECUDA = 2,        /* a CUDA runtime call failed                                      */
     LBM_ENAN = 3,         /* a reduction found a non-finite value                            */
-    LBM_ETIMEOUT = 4,     /* reserved for a bounded device wait that gives up; no kernel of  */
-                          /* this library waits on another, so no entry point returns it     */
+    LBM_ETIMEOUT = 4,     /* a bounded device wait gave up (the staged kernel's wait for its  */
+                          /* bulk copies; reported by lbm_device_status)                     */
     LBM_ENOMEM = 5,       /* a handle-owned allocation failed                                */
     LBM_EUNSUPPORTED = 6  /* the combination is not built (e.g. IBB with esoteric pull)      */
 } lbm_status;
@@ -149,15 +149,28 @@ lbm_status lbm_set_block_threads(lbm_handle* h, int32_t threads);
  * 0 = automatic (default), 1 = the generic kernel (any tile), 2 = the block-per-tile kernel,
  * which needs 256-cell tiles with power-of-two sides and Q*N < 2^31, 3 = the cell-pair
  * block-per-tile kernel (one thread per two cells along x, word-wide population accesses), which
- * also needs the double-buffer method and tx >= 2 (LBM_EUNSUPPORTED otherwise); a step whose
- * population buffers are not 8-byte aligned, or a handle with the learned closure, runs the
- * block-per-tile kernel instead.  With LBM_ARITH_EXACT all produce identical populations; the
+ * also needs the double-buffer method and tx >= 2, 4 = the staged block-per-tile kernel (persistent
+ * CTAs; bulk asynchronous copies stage the next tile's pull neighbourhood in shared memory while
+ * the current tile is stepped), which needs the double-buffer method and tile rows of a multiple of
+ * 16 bytes (tx >= 8 Float16C, tx >= 4 float32) (LBM_EUNSUPPORTED otherwise).  A step whose
+ * population buffers are not 8-byte (path 3) or 16-byte (path 4) aligned, or a handle with the
+ * learned closure or fused links, runs the block-per-tile kernel (or its variant) instead.  With LBM_ARITH_EXACT all produce identical populations; the
  * generic kernel always computes the exact arithmetic. */
 lbm_status lbm_set_kernel_path(lbm_handle* h, int32_t path);
 
 /* The kernel lbm_*_step will use (aligned buffers): 1 generic, 2 block-per-tile, 3 cell-pair,
- * -1 for a null handle. */
+ * 4 staged, -1 for a null handle. */
 int32_t lbm_kernel_path(const lbm_handle* h);
+
+/* Waits for the device and reports the errors the kernels raised on the device since the last
+ * call (no counterpart in the reference, whose kernels report nothing): LBM_ETIMEOUT when a wait of
+ * the staged kernel for its bulk copies ran out (0.5 s); the steps it had not finished are lost
+ * and the error is cleared.  LBM_OK otherwise. */
+lbm_status lbm_device_status(lbm_handle* h);
+
+/* Test hook (no counterpart in the reference): adds `bytes` (a multiple of 16) to the byte count
+ * each stage of the staged kernel waits for, so that its bounded wait runs out; 0 restores it. */
+lbm_status lbm_debug_stage_extra_bytes(lbm_handle* h, uint32_t bytes);
 
 /* ---- the step ---- */
 

@@ -71,6 +71,9 @@ SIGNATURES = {
     "lbm_set_block_threads": (_i32, [_vp, _i32]),
     "lbm_set_kernel_path": (_i32, [_vp, _i32]),
     "lbm_kernel_path": (_i32, [_vp]),
+    "lbm_device_status": (_i32, [_vp]),
+    "lbm_debug_stage_extra_bytes": (_i32, [_vp, C.c_uint32]),
+    "lbm_stage_segments": (_i32, [_i32, _i32, _i32, _i32, _i32, _vp, _i32, _vp]),
     "lbm_double_buffer_step": (_i32, [_vp, _vp, _vp, _vp, _vp, _f32, _vp]),
     "lbm_esoteric_pull_step": (_i32, [_vp, _vp, _vp, _vp, _f32, _i32, _vp]),
     "lbm_run": (_i32, [_vp, _vp, _vp, _vp, _vp, _f32, _i64, _i64, _vp]),

@@ -13,6 +13,7 @@
 
 #include "lbm_aux.cuh"
 #include "lbm_link_tables.h"
+#include "lbm_stage.cuh"
 
 namespace lbm {
 StepLaunch get_step_d2q9(int, int, int, int);
@@ -28,6 +29,10 @@ StepLaunch get_pair_step_d2q9(int, int, int, int);
 StepLaunch get_pair_step_d3q19(int, int, int, int);
 StepLaunch get_pair_step_d3q27(int, int, int, int);
 StepLaunch get_links_tile_step_d2q9(int, int, int, int);
+StepLaunch get_staged_step_d2q9(int, int, int, int);
+StepLaunch get_staged_step_d3q19(int, int, int, int);
+StepLaunch get_staged_step_d3q27(int, int, int, int);
+std::vector<StageSeg> build_stage_segments(int lattice, int tx, int ty, int tz, int esz, uint32_t* stage_bytes);
 StepLaunch get_links_tile_step_d3q19(int, int, int, int);
 StepLaunch get_links_tile_step_d3q27(int, int, int, int);
 StepLaunch get_learned_step_d2q9(int, int, int);
@@ -108,7 +113,11 @@ struct lbm_handle {
     StepLaunch step_learned;  // block-per-tile kernel with the learned closure (LES handles), or null
     StepLaunch step_pair;  // cell-pair block-per-tile kernel (double buffer, tx >= 2), or null
     StepLaunch step_links;    // block-per-tile kernel with fused links (double buffer), or null
-    int path;              // 0 auto, 1 generic only, 2 block-per-tile only, 3 cell-pair
+    StepLaunch step_staged;   // staged block-per-tile kernel (double buffer, 16-byte tile rows), or null
+    int path;              // 0 auto, 1 generic only, 2 block-per-tile only, 3 cell-pair, 4 staged
+    StageSeg* stage_segs;  // the staged kernel's copy segments (device), or null
+    uint32_t nsegs, stage_bytes, stage_extra;
+    uint32_t* dev_err;     // device word raised by the staged kernel's bounded waits
     uint8_t* box_sum;      // per warp box (32 cells): summary byte (flags other than 0 inside, on faces)
     uint2* cell_masks;     // per cell: neighbour-solid masks, written for the warps with a mask bit set
     uint8_t* flags_seen;   // the flags the summary was built from
@@ -192,10 +201,20 @@ StepArgs step_args(const lbm_handle* h, const void* f_in, void* f_out, float* bc
     a.link_stride = h->n_links;
     a.q_clamp = h->q_clamp;
     a.bouzidi = h->bouzidi;
+    a.stage_segs = h->stage_segs;
+    a.nsegs = h->nsegs;
+    a.stage_bytes = h->stage_bytes;
+    a.err = h->dev_err;
+    a.stage_extra = h->stage_extra;
     return a;
 }
 
 bool use_tile(const lbm_handle* h) { return h->step_tile != nullptr && h->path != 1; }
+
+// The staged kernel is chosen (path 4) and can run: no learned closure, no fused links.
+bool use_staged(const lbm_handle* h) {
+    return h->path == 4 && h->step_staged != nullptr && !h->closure_on && !h->link_table;
+}
 
 // The cell-pair kernel is chosen (path 3) and can run: no learned closure, no fused links.
 bool use_pair(const lbm_handle* h) {
@@ -209,6 +228,8 @@ StepLaunch step_fn(const lbm_handle* h, const StepArgs& a) {
     if (!use_tile(h)) return h->step;
     if (h->closure_on) return h->step_learned;
     if (h->link_table) return h->step_links;
+    const uintptr_t al = reinterpret_cast<uintptr_t>(a.f_in) | reinterpret_cast<uintptr_t>(a.f_out);
+    if (use_staged(h) && (al & 15u) == 0u) return h->step_staged;  // bulk copies: 16-byte aligned rows
     if (use_pair(h) && ((reinterpret_cast<uintptr_t>(a.f_in) | reinterpret_cast<uintptr_t>(a.f_out)) & 7u) == 0u)
         return h->step_pair;
     return h->step_tile;
@@ -371,6 +392,19 @@ lbm_status lbm_create(const lbm_config_t* cfg, const lbm_grid_t* grid, lbm_handl
                   : grid->lattice == LBM_D2Q9 ? get_links_tile_step_d2q9(f16, co, les, fast)
                   : grid->lattice == LBM_D3Q19 ? get_links_tile_step_d3q19(f16, co, les, fast)
                                                : get_links_tile_step_d3q27(f16, co, les, fast);
+    const int esz = f16 ? 2 : 4;
+    std::vector<StageSeg> segs;
+    h->stage_bytes = 0;
+    if (tile_ok && m == LBM_DOUBLE_BUFFER)
+        segs = build_stage_segments(grid->lattice, grid->tx, grid->ty, grid->tz, esz, &h->stage_bytes);
+    h->nsegs = (uint32_t)segs.size();
+    h->stage_extra = 0;
+    h->stage_segs = nullptr;
+    h->dev_err = nullptr;
+    h->step_staged = segs.empty() ? nullptr
+                   : grid->lattice == LBM_D2Q9 ? get_staged_step_d2q9(f16, co, les, fast)
+                   : grid->lattice == LBM_D3Q19 ? get_staged_step_d3q19(f16, co, les, fast)
+                                                : get_staged_step_d3q27(f16, co, les, fast);
     h->path = 0;
     h->ntiles = h->lay.ncells / h->lay.T;
     h->mx = (uint32_t)grid->tx - 1u;
@@ -407,6 +441,11 @@ lbm_status lbm_create(const lbm_config_t* cfg, const lbm_grid_t* grid, lbm_handl
     if (e == cudaSuccess && h->step_tile) e = cudaMalloc(&h->changed, sizeof(uint32_t));
     if (e == cudaSuccess && h->step_tile) e = cudaMemset(h->changed, 0, sizeof(uint32_t));
     if (e == cudaSuccess && h->step_tile) e = cudaMalloc(&h->tile_near, h->ntiles);
+    if (e == cudaSuccess) e = cudaMalloc(&h->dev_err, sizeof(uint32_t));
+    if (e == cudaSuccess) e = cudaMemset(h->dev_err, 0, sizeof(uint32_t));
+    if (e == cudaSuccess && !segs.empty()) e = cudaMalloc(&h->stage_segs, sizeof(StageSeg) * segs.size());
+    if (e == cudaSuccess && !segs.empty())
+        e = cudaMemcpy(h->stage_segs, segs.data(), sizeof(StageSeg) * segs.size(), cudaMemcpyHostToDevice);
     if (e != cudaSuccess) {
         lbm_destroy(h);
         return fail(LBM_ECUDA, std::string("lbm_create: ") + cudaGetErrorString(e));
@@ -428,6 +467,8 @@ lbm_status lbm_destroy(lbm_handle* h) {
     if (h->link_table) cudaFree(h->link_table);
     if (h->link_dist) cudaFree(h->link_dist);
     if (h->link_id) cudaFree(h->link_id);
+    if (h->stage_segs) cudaFree(h->stage_segs);
+    if (h->dev_err) cudaFree(h->dev_err);
     if (h->capture_stream) cudaStreamDestroy(h->capture_stream);
     delete h;
     return LBM_OK;
@@ -527,8 +568,12 @@ lbm_status lbm_set_block_threads(lbm_handle* h, int32_t threads) {
 
 lbm_status lbm_set_kernel_path(lbm_handle* h, int32_t path) {
     if (check_handle(h)) return LBM_EINVAL;
-    if (path < 0 || path > 3)
-        return fail(LBM_EINVAL, "path must be 0 (auto), 1 (generic), 2 (block-per-tile) or 3 (cell-pair)");
+    if (path < 0 || path > 4)
+        return fail(LBM_EINVAL, "path must be 0 (auto), 1 (generic), 2 (block-per-tile), 3 (cell-pair) or 4 (staged)");
+    if (path == 4 && !h->step_staged)
+        return fail(LBM_EUNSUPPORTED, "the staged kernel needs the double-buffer method, 256-cell power-of-two tiles "
+                                      "whose rows are multiples of 16 bytes (tx >= 8 Float16C, tx >= 4 float32) and "
+                                      "Q*N < 2^31");
     if (path == 2 && !h->step_tile)
         return fail(LBM_EUNSUPPORTED, "the block-per-tile kernel needs 256-cell power-of-two tiles and Q*N < 2^31");
     if (path == 3 && !h->step_pair)
@@ -542,7 +587,29 @@ lbm_status lbm_set_kernel_path(lbm_handle* h, int32_t path) {
     return LBM_OK;
 }
 
-int32_t lbm_kernel_path(const lbm_handle* h) { return h ? (use_tile(h) ? (use_pair(h) ? 3 : 2) : 1) : -1; }
+int32_t lbm_kernel_path(const lbm_handle* h) {
+    return h ? (use_tile(h) ? (use_staged(h) ? 4 : use_pair(h) ? 3 : 2) : 1) : -1;
+}
+
+lbm_status lbm_device_status(lbm_handle* h) {
+    if (check_handle(h)) return LBM_EINVAL;
+    LBM_CK(cudaDeviceSynchronize());
+    uint32_t v = 0;
+    LBM_CK(cudaMemcpy(&v, h->dev_err, sizeof(v), cudaMemcpyDeviceToHost));
+    if (v == 0u) return LBM_OK;
+    LBM_CK(cudaMemset(h->dev_err, 0, sizeof(uint32_t)));
+    return fail(LBM_ETIMEOUT, "a staged step's wait for its bulk copies ran out of time; the tiles it had not "
+                              "reached were not stepped");
+}
+
+lbm_status lbm_debug_stage_extra_bytes(lbm_handle* h, uint32_t bytes) {
+    if (check_handle(h)) return LBM_EINVAL;
+    if (bytes % 16u) return fail(LBM_EINVAL, "extra bytes must be a multiple of 16");
+    h->stage_extra = bytes;
+    for (auto& kv : h->graphs) cudaGraphExecDestroy(kv.second);
+    h->graphs.clear();
+    return LBM_OK;
+}
 
 lbm_status lbm_double_buffer_step(lbm_handle* h, void* f_out, const void* f_in, float* bc, const uint8_t* flags,
                                   float tau, void* stream) {
@@ -596,7 +663,7 @@ lbm_status lbm_run(lbm_handle* h, void* f_a, void* f_b, float* bc, const uint8_t
     if (n_steps >= chunk) {
         uint32_t tau_bits;
         std::memcpy(&tau_bits, &tau, 4);
-        const GraphKey key{f_a, f_b, bc, flags, tau_bits, (int)(first_step % 2), chunk, use_tile(h) ? (use_pair(h) ? 3 : 2) : 1};
+        const GraphKey key{f_a, f_b, bc, flags, tau_bits, (int)(first_step % 2), chunk, use_tile(h) ? (use_staged(h) ? 4 : use_pair(h) ? 3 : 2) : 1};
         auto it = h->graphs.find(key);
         if (it == h->graphs.end()) {
             cudaGraph_t g = nullptr;

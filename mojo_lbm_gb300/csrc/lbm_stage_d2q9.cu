@@ -1,0 +1,11 @@
+// The 32 double-buffer staged fused-step variants of the D2Q9 lattice (lbm_stage.cuh), exact and
+// fast arithmetic.
+#include "lbm_stage.cuh"
+
+namespace lbm {
+StepLaunch get_staged_step_d2q9(int f16c, int coll, int les, int fast) {
+    static const StepLaunch exact[16] = LBM_DB_TABLE(launch_step_staged, D2Q9);
+    static const StepLaunch fastt[16] = LBM_DB_TABLE(launch_step_staged_fast, D2Q9);
+    return (fast ? fastt : exact)[db_index(f16c, coll, les)];
+}
+}  // namespace lbm

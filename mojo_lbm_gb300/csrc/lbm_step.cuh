@@ -49,6 +49,13 @@ struct StepArgs {
     int64_t link_stride;
     float q_clamp;
     int32_t bouzidi;
+    // staged kernel (lbm_stage.cuh): its copy segments, the bytes they move per tile, the device
+    // word its bounded waits raise on a timeout, and bytes added to each stage's expected count
+    // (0; a test raises it to make the wait run out)
+    const void* stage_segs;
+    uint32_t nsegs, stage_bytes;
+    uint32_t* err;
+    uint32_t stage_extra;
 };
 
 // Storage traits: float32, or Float16C codes decoded to float32 (load_f / store_f,
@@ -834,6 +841,21 @@ __device__ __forceinline__ void tile_cell_masks(const StepArgs& a, uint32_t tile
     masks[n] = cell_solid_masks<L>(a.flags, n, dc);
 }
 
+// The shared-memory stage of the staged kernel (lbm_stage.cuh): per direction q, in q order, a region
+// of 256 populations (c_q.x = 0) or 512 (c_q.x != 0: the rows of the tile's own column, then those
+// of its x-neighbour column).  Position t of a region holds the row the cell t of the tile pulls
+// from, shifted by -c_q.y, -c_q.z (from the y/z-neighbour tiles at the tile's faces); along x the
+// cell reads position t - c_q.x of the first half, or at the tile's x edge the x-neighbour's cell in
+// the second half.
+template <class L>
+constexpr LBM_HD uint32_t stage_elems(int q) { return L::c(q, 0) == 0 ? kTileCells : 2u * kTileCells; }
+template <class L>
+constexpr LBM_HD uint32_t stage_off(int q) {
+    uint32_t o = 0;
+    for (int p = 0; p < q; ++p) o += stage_elems<L>(p);
+    return o;
+}
+
 // Interpolated bounce-back fused into the step: the node-wise form of the reference's WIP kernel
 // (src/lbm/geometry/nodewise_interpolated_BB.mojo:46-185) with the interpolation of its working
 // link-wise kernel (geometry/interpolated_BB.mojo:102-141), so that the fused step reproduces the
@@ -901,10 +923,13 @@ __device__ __forceinline__ void fused_links(float (&f)[L::Q], const uint2 lt, co
 // when the collision is linear in f.  LINKS: the interpolated bounce-back of the links in
 // a.link_table fused into the stream (fused_links; double buffer).  It is a separate build because
 // its code would raise the register demand of every kernel beyond the budget of 5 CTAs per SM.
-template <class L, int METHOD, bool F16C, int COLL, int LES, bool FAST = false, bool LINKS = false>
+// STAGED: the pull loads read the tile's shared-memory stage `stage` (stage_off; double buffer)
+// instead of global memory.
+template <class L, int METHOD, bool F16C, int COLL, int LES, bool FAST = false, bool LINKS = false,
+          bool STAGED = false>
 __device__ __forceinline__ void tile_step(const StepArgs& a, const uint32_t tile, const uint32_t tid,
                                           const ClosureDev* cl = nullptr, float4* fbuf = nullptr,
-                                          int32_t near = -1) {
+                                          int32_t near = -1, const void* stage = nullptr) {
     using P = Pop<F16C>;
     using S = typename P::T;
     constexpr int Q = L::Q, D = L::D, K = D + 1;
@@ -912,6 +937,7 @@ __device__ __forceinline__ void tile_step(const StepArgs& a, const uint32_t tile
     constexpr bool ESO = METHOD == LBM_ESOTERIC_PULL;
     static_assert(!(FAST && LES == kLesLearned), "the learned closure has its own tolerance build");
     static_assert(!(LINKS && ESO), "the fused links are double-buffer only");
+    static_assert(!(STAGED && ESO), "the staged kernel is double-buffer only");
     constexpr bool SCALED = FAST && F16C && !LES && COLL != LBM_KBC;
     auto ld = [](const S* p) -> float {
         if constexpr (SCALED) return P::ld_scaled(p);
@@ -961,7 +987,21 @@ __device__ __forceinline__ void tile_step(const StepArgs& a, const uint32_t tile
 
     // ---- stream (pull loads first, independent of the flags)
     float f[Q];
-    if constexpr (!ESO) {
+    if constexpr (STAGED) {
+        // the stage's regions: this cell's position, or along x the neighbour's (stage_off)
+        const S* sp = static_cast<const S*>(stage);
+        const int32_t t = (int32_t)tid;
+        const int32_t bm = lx >= 1u ? t - 1 : t + (int32_t)T + tx - 1;         // source x - 1
+        const int32_t bp = (int32_t)lx + 2 <= tx ? t + 1 : t + (int32_t)T - tx + 1;  // source x + 1
+        static_for<0, Q>([&](auto qc) {
+            constexpr int q = qc.value, cx = L::c(q, 0);
+            constexpr uint32_t off = stage_off<L>(q);
+            const int32_t b = cx == 0 ? t : (cx > 0 ? bm : bp);
+            if constexpr (!F16C) f[q] = sp[off + b];
+            else if constexpr (SCALED) f[q] = f16c_decode_scaled_sx(reinterpret_cast<const int16_t*>(sp)[off + b]);
+            else f[q] = f16c_decode_sx(reinterpret_cast<const int16_t*>(sp)[off + b]);
+        });
+    } else if constexpr (!ESO) {
         static_for<0, Q>([&](auto qc) {
             constexpr int q = qc.value;
             constexpr int sx = -L::c(q, 0), sy = -L::c(q, 1), sz = -L::c(q, 2);

@@ -44,13 +44,19 @@ class Solver:
         check(self._lib.lbm_set_block_threads(self._h, int(threads)))
 
     def set_kernel_path(self, path: int) -> None:
-        """0 automatic, 1 generic kernel, 2 block-per-tile kernel, 3 cell-pair block-per-tile kernel
-        (double buffer; identical results in the exact arithmetic)."""
+        """0 automatic, 1 generic kernel, 2 block-per-tile kernel, 3 cell-pair block-per-tile kernel,
+        4 staged block-per-tile kernel (3 and 4: double buffer; identical results in the exact
+        arithmetic)."""
         check(self._lib.lbm_set_kernel_path(self._h, int(path)))
 
     @property
     def kernel_path(self) -> int:
         return int(self._lib.lbm_kernel_path(self._h))
+
+    def device_status(self) -> None:
+        """Waits for the device; raises on an error a kernel reported on the device (LBM_ETIMEOUT:
+        the staged kernel's bounded wait for its bulk copies ran out)."""
+        check(self._lib.lbm_device_status(self._h))
 
     # -- the step (solver.mojo:81-154) ------------------------------------------------------
     def double_buffer_step(self, f_out, f_in, bc, flags, tau: float, stream=None) -> None:
