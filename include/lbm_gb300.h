@@ -172,6 +172,13 @@ lbm_status lbm_device_status(lbm_handle* h);
  * each stage of the staged kernel waits for, so that its bounded wait runs out; 0 restores it. */
 lbm_status lbm_debug_stage_extra_bytes(lbm_handle* h, uint32_t bytes);
 
+/* Test hook (no counterpart in the reference): the staged kernel's copy segments for a tile shape
+ * (lattice, tx, ty, tz, bytes per population esz) as (source element, destination byte, bytes,
+ * neighbour code) quadruples in out (at most max_segs); returns their count and the bytes of one
+ * stage in *stage_bytes, 0 for a shape whose tile rows are not 16-byte multiples. */
+int32_t lbm_stage_segments(int32_t lattice, int32_t tx, int32_t ty, int32_t tz, int32_t esz, uint32_t* out,
+                           int32_t max_segs, uint32_t* stage_bytes);
+
 /* ---- the step ---- */
 
 /* Solver.double_buffer_step (solver.mojo:81-111) -> double_buffer_kernel

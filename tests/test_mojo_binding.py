@@ -16,7 +16,7 @@ ROOT = Path(__file__).resolve().parents[1]
 HEADER = ROOT / "include" / "lbm_gb300.h"
 BINDING = ROOT / "mojo_lbm_gb300" / "mojo" / "gb300.mojo"
 
-SCALARS = {"int32_t": "Int32", "int64_t": "Int64", "float": "Float32", "uint8_t": "UInt8", "lbm_status": "Int32"}
+SCALARS = {"int32_t": "Int32", "int64_t": "Int64", "float": "Float32", "uint8_t": "UInt8", "uint32_t": "UInt32", "lbm_status": "Int32"}
 
 
 def _strip_c_comments(s: str) -> str:
