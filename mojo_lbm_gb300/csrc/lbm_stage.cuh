@@ -75,28 +75,34 @@ __device__ __forceinline__ void bulk_copy_g2s(uint32_t dst, const void* src, uin
                  : "memory");
 }
 
-// Warp 0 issues the stage of `tile` into the buffer at shared address `buf`, completing on `bar`.
-template <class L, bool F16C>
-__device__ __forceinline__ void stage_issue(const StepArgs& a, const StageSeg* segs, uint32_t tile, uint32_t buf,
-                                            uint32_t bar, uint32_t lane) {
-    using S = typename Pop<F16C>::T;
-    if (lane == 0u) mbar_expect_tx(bar, a.stage_bytes + a.stage_extra);
-    __syncwarp();
-    fence_proxy_async_smem();
+// Index of the neighbour tile (nbr % 3, nbr / 3 % 3, nbr / 9) - 1 of `tile`, with the periodic wrap.
+__device__ __forceinline__ uint32_t stage_nbr_tile(const StepArgs& a, uint32_t tile, uint32_t nbr) {
     const uint32_t ntx = (uint32_t)a.lay.ntx, nty = (uint32_t)a.lay.nty, ntz = (uint32_t)a.lay.ntz;
     const uint32_t byz = a.lay.d_ntx.div(tile);
     const uint32_t bx = tile - byz * ntx;
     const uint32_t bz = a.lay.d_nty.div(byz);
     const uint32_t by = byz - bz * nty;
+    const uint32_t ox = nbr % 3u, oy = (nbr / 3u) % 3u, oz = nbr / 9u;  // offset + 1
+    const uint32_t x = ox == 0u ? (bx == 0u ? ntx - 1u : bx - 1u) : ox == 2u ? (bx + 1u == ntx ? 0u : bx + 1u) : bx;
+    const uint32_t y = oy == 0u ? (by == 0u ? nty - 1u : by - 1u) : oy == 2u ? (by + 1u == nty ? 0u : by + 1u) : by;
+    const uint32_t z = oz == 0u ? (bz == 0u ? ntz - 1u : bz - 1u) : oz == 2u ? (bz + 1u == ntz ? 0u : bz + 1u) : bz;
+    return x + ntx * (y + nty * z);
+}
+
+// The stage's copies into the buffer at shared address `buf`, completing on `bar`, from the tiles
+// nbr[0..26]; spread over the CTA's warps (segment i goes to warp i % 8), since the copy
+// instruction takes its operands from uniform registers and a warp issues its lanes' copies one
+// after another.
+template <class L, bool F16C>
+__device__ __forceinline__ void stage_copies(const StepArgs& a, const StageSeg* segs, const uint32_t* nbr,
+                                             uint32_t buf, uint32_t bar, uint32_t tid) {
+    using S = typename Pop<F16C>::T;
     const S* f = static_cast<const S*>(a.f_in);
-    for (uint32_t i = lane; i < a.nsegs; i += 32u) {
+    fence_proxy_async_smem();
+    constexpr uint32_t W = kTileCells / 32u;
+    for (uint32_t i = (tid >> 5) + W * (tid & 31u); i < a.nsegs; i += kTileCells) {
         const StageSeg s = segs[i];
-        const uint32_t ox = s.nbr % 3u, oy = (s.nbr / 3u) % 3u, oz = s.nbr / 9u;  // offset + 1
-        const uint32_t x = ox == 0u ? (bx == 0u ? ntx - 1u : bx - 1u) : ox == 2u ? (bx + 1u == ntx ? 0u : bx + 1u) : bx;
-        const uint32_t y = oy == 0u ? (by == 0u ? nty - 1u : by - 1u) : oy == 2u ? (by + 1u == nty ? 0u : by + 1u) : by;
-        const uint32_t z = oz == 0u ? (bz == 0u ? ntz - 1u : bz - 1u) : oz == 2u ? (bz + 1u == ntz ? 0u : bz + 1u) : bz;
-        const uint64_t t = (uint64_t)x + (uint64_t)ntx * ((uint64_t)y + (uint64_t)nty * z);
-        bulk_copy_g2s(buf + s.dst, f + t * (uint64_t)(kTileCells * L::Q) + s.src, s.bytes, bar);
+        bulk_copy_g2s(buf + s.dst, f + (uint64_t)nbr[s.nbr] * (uint64_t)(kTileCells * L::Q) + s.src, s.bytes, bar);
     }
 }
 
@@ -120,44 +126,63 @@ template <class L, bool F16C, int COLL, int LES, bool FAST>
 __global__ void __launch_bounds__(kTileCells, (stage_min_blocks<L, COLL>())) step_kernel_staged(const StepArgs a) {
     static_assert(LES != kLesLearned, "the learned closure runs in step_kernel_learned");
     extern __shared__ __align__(128) uint8_t smem[];
-    const uint32_t tid = threadIdx.x, lane = tid & 31u;
+    __shared__ uint32_t nbr[2][27];  // the neighbour tiles of the tile each buffer is staging
+    const uint32_t tid = threadIdx.x;
     StageSeg* segs = reinterpret_cast<StageSeg*>(smem + kStageHead);
-    uint8_t* buf0 = smem + kStageHead + ((a.nsegs * (uint32_t)sizeof(StageSeg) + 127u) & ~127u);
-    uint8_t* buf1 = buf0 + a.stage_bytes;
+    uint8_t* const buf0 = smem + kStageHead + ((a.nsegs * (uint32_t)sizeof(StageSeg) + 127u) & ~127u);
+    uint8_t* const buf1 = buf0 + a.stage_bytes;
     const uint32_t bar0 = smem_u32(smem), bar1 = bar0 + 8u;
     const uint32_t ntiles = a.lay.ncells / kTileCells;
+    const uint32_t G = gridDim.x;
+    uint32_t tile = blockIdx.x;
+    if (tile >= ntiles) return;
 
+    // prologue: the segment list, the barriers, the stages of the first two tiles
     const uint32_t* src = static_cast<const uint32_t*>(a.stage_segs);
     for (uint32_t i = tid; i < a.nsegs * 4u; i += kTileCells) reinterpret_cast<uint32_t*>(segs)[i] = __ldg(src + i);
+    const bool second = tile + G < ntiles;
+    if (tid < 27u) {
+        nbr[0][tid] = stage_nbr_tile(a, tile, tid);
+        if (second) nbr[1][tid] = stage_nbr_tile(a, tile + G, tid);
+    }
     if (tid == 0u) {
         mbar_init(bar0, 1u);
         mbar_init(bar1, 1u);
         mbar_fence_init();
+        mbar_expect_tx(bar0, a.stage_bytes + a.stage_extra);
+        if (second) mbar_expect_tx(bar1, a.stage_bytes + a.stage_extra);
     }
     __syncthreads();
-    uint32_t tile = blockIdx.x;
-    if (tile >= ntiles) return;
-    if (tid < 32u) stage_issue<L, F16C>(a, segs, tile, smem_u32(buf0), bar0, lane);
+    stage_copies<L, F16C>(a, segs, nbr[0], smem_u32(buf0), bar0, tid);
+    if (second) stage_copies<L, F16C>(a, segs, nbr[1], smem_u32(buf1), bar1, tid);
+
     for (uint32_t k = 0;; ++k) {
         const uint32_t s = k & 1u;
-        const uint32_t next = tile + gridDim.x;
-        // the other buffer was last read in iteration k - 1, which every thread has left
-        if (next < ntiles && tid < 32u) stage_issue<L, F16C>(a, segs, next, smem_u32(s ? buf0 : buf1), s ? bar0 : bar1, lane);
-        const bool ok = mbar_wait(s ? bar1 : bar0, (k >> 1) & 1u);
+        const uint32_t bar_s = s ? bar1 : bar0, bar_o = s ? bar0 : bar1;
+        uint8_t* const buf_s = s ? buf1 : buf0;
+        const bool ok = mbar_wait(bar_s, (k >> 1) & 1u);
         if (__syncthreads_or(!ok)) {
             // timed out: report, let the copies in flight land (bounded), leave
             if (tid == 0u) {
                 atomicExch(a.err, 1u);
-                mbar_wait(s ? bar1 : bar0, (k >> 1) & 1u);
-                if (next < ntiles) mbar_wait(s ? bar0 : bar1, ((k + 1) >> 1) & 1u);
+                mbar_wait(bar_s, (k >> 1) & 1u);
+                if (tile + G < ntiles) mbar_wait(bar_o, ((k + 1) >> 1) & 1u);
             }
             return;
         }
         tile_step<L, LBM_DOUBLE_BUFFER, F16C, COLL, LES, FAST, false, true>(a, tile, tid, nullptr, nullptr, -1,
-                                                                          s ? buf1 : buf0);
+                                                                          buf_s);
+        // buffer s next stages the tile two ahead, once every thread has read it
+        const uint32_t ahead = tile + 2u * G;
+        const bool more = ahead < ntiles;
+        if (more) {
+            if (tid < 27u) nbr[s][tid] = stage_nbr_tile(a, ahead, tid);
+            if (tid == 0u) mbar_expect_tx(bar_s, a.stage_bytes + a.stage_extra);
+        }
         __syncthreads();
-        if (next >= ntiles) break;
-        tile = next;
+        if (more) stage_copies<L, F16C>(a, segs, nbr[s], smem_u32(buf_s), bar_s, tid);
+        if (tile + G >= ntiles) break;
+        tile += G;
     }
 }
 
