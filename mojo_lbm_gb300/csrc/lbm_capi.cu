@@ -112,6 +112,7 @@ struct lbm_handle {
     StepLaunch step_tile;  // block-per-tile kernel, or null when the grid does not qualify
     StepLaunch step_learned;  // block-per-tile kernel with the learned closure (LES handles), or null
     StepLaunch step_pair;  // cell-pair block-per-tile kernel (double buffer, tx >= 2), or null
+    int pair_auto;         // the automatic choice takes the cell-pair kernel
     StepLaunch step_links;    // block-per-tile kernel with fused links (double buffer), or null
     StepLaunch step_staged;   // staged block-per-tile kernel (double buffer, 16-byte tile rows), or null
     int path;              // 0 auto, 1 generic only, 2 block-per-tile only, 3 cell-pair, 4 staged
@@ -217,8 +218,12 @@ bool use_staged(const lbm_handle* h) {
 }
 
 // The cell-pair kernel is chosen (path 3) and can run: no learned closure, no fused links.
+// The automatic choice (path 0) takes it where it measured faster than the per-cell kernel: the
+// double-buffer D2Q9 / D3Q19 configurations other than KBC (whose larger register demand halves the
+// pair kernel's occupancy).
 bool use_pair(const lbm_handle* h) {
-    return h->path == 3 && h->step_pair != nullptr && !h->closure_on && !h->link_table;
+    return (h->path == 3 || (h->path == 0 && h->pair_auto)) && h->step_pair != nullptr && !h->closure_on &&
+           !h->link_table;
 }
 
 // The kernel the next step with these arguments runs.  The cell-pair kernel moves 8-byte
@@ -405,6 +410,7 @@ lbm_status lbm_create(const lbm_config_t* cfg, const lbm_grid_t* grid, lbm_handl
                    : grid->lattice == LBM_D2Q9 ? get_staged_step_d2q9(f16, co, les, fast)
                    : grid->lattice == LBM_D3Q19 ? get_staged_step_d3q19(f16, co, les, fast)
                                                 : get_staged_step_d3q27(f16, co, les, fast);
+    h->pair_auto = h->step_pair != nullptr && co != LBM_KBC && grid->lattice != LBM_D3Q27;
     h->path = 0;
     h->ntiles = h->lay.ncells / h->lay.T;
     h->mx = (uint32_t)grid->tx - 1u;

@@ -87,7 +87,7 @@ def _run_linkwise(grid, cfg, flags, bc, f0, body, method, tau, steps):
 
 def _run_fused(grid, cfg, flags, bc, f0, body, method, tau, steps, by_run=False):
     s = Solver(grid, cfg)
-    assert s.kernel_path == 2
+    assert s.kernel_path in (2, 3)
     fa, fb, bct, flt = _dev(f0), _dev(f0), _dev(bc), _dev(flags)
     ids, dirs, dists = _links(body)
     force = torch.zeros(ids.numel() * grid.D, device="cuda")

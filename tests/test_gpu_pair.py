@@ -127,8 +127,10 @@ def test_pair_path_selection():
     s = Solver(make_grid("D3Q19", (16, 16, 8), (8, 8, 4)), LBM_Config())
     s.set_kernel_path(3)
     assert s.kernel_path == 3
-    s.set_kernel_path(0)
+    s.set_kernel_path(2)
     assert s.kernel_path == 2
+    s.set_kernel_path(0)
+    assert s.kernel_path == 3  # the automatic choice for D3Q19 SRT
     s.close()
     for grid, cfg in ((make_grid("D3Q19", (16, 16, 8), (8, 8, 4)), LBM_Config(LBM_method.ESOTERIC_PULL)),
                       (make_grid("D3Q19", (16, 64, 8), (1, 64, 4)), LBM_Config()),
