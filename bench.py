@@ -41,11 +41,11 @@ WORKLOADS = {
                                  desc="D3Q19 SRT lid-driven cube 256^3, FP32/FP32, Re=100, lid u=0.1, "
                                       "two-lattice pull streaming (double buffer)"),
     "ldc3d_d3q19_256_f16c": dict(lattice="D3Q19", n=256, method="db", coll="SRT", les=False, f16=True, Re=100.0,
-                                 U=0.1, tile=(8, 8, 4),
+                                 U=0.1, tile=(8, 8, 4), arith="fast",
                                  desc="D3Q19 SRT lid-driven cube 256^3, Float16C storage + DDF shift, FP32 math, "
                                       "Re=100, lid u=0.1, pull streaming"),
     "ldc3d_d3q27_256_kbc_f16c_eso": dict(lattice="D3Q27", n=256, method="eso", coll="KBC", les=True, f16=True,
-                                         Re=10000.0, U=0.1, tile=(8, 8, 4),
+                                         Re=10000.0, U=0.1, tile=(8, 8, 4), arith="fast",
                                          desc="D3Q27 KBC + Smagorinsky Cs=0.1 lid-driven cube 256^3, Re=10000, "
                                               "Float16C + DDF shift, FP32 math, esoteric-pull in place"),
     # the reference's CPU-runnable configuration (its 2D cavity examples, examples/LDC.mojo)
@@ -66,7 +66,7 @@ WORKLOADS = {
 for _f16, _pub in ((False, 2212.0), (True, 2776.0)):
     WORKLOADS[f"periodic256_d3q19_{'f16c' if _f16 else 'fp32'}_rest"] = dict(
         kind="rest", lattice="D3Q19", n=256, method="db", coll="SRT", les=False, f16=_f16, tau=0.884,
-        tile=(8, 8, 4), published_mlups=_pub,
+        tile=(8, 8, 4), published_mlups=_pub, **({"arith": "fast"} if _f16 else {}),
         desc="D3Q19 SRT periodic 256^3 at rest, tau=0.884, " + ("Float16C storage + DDF shift, FP32 math"
                                                                 if _f16 else "FP32/FP32")
              + ", pull streaming (double buffer): the reference's published benchmark configuration")
