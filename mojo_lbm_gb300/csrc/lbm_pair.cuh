@@ -55,15 +55,19 @@ template <bool SCALED> struct PairWord<true, SCALED> {
         }
     }
     static __device__ __forceinline__ void st(uint16_t* p, float a, float b) {
-        uint32_t ca, cb;
+        uint32_t w;
         if constexpr (SCALED) {
-            ca = f16c_encode_scaled(a);
-            cb = f16c_encode_scaled(b);
+            // f16c_encode_scaled of both: the two magnitudes side by side, then both signs (the top
+            // bytes of a and b moved to bytes 1 and 3, bits 15 and 31 kept) in one bitwise select
+            constexpr float kSatScaled = 0x1.ffdp-112f;
+            const uint32_t ma = round_shift12(as_u32(fminf(fabsf(a), kSatScaled)));
+            const uint32_t mb = round_shift12(as_u32(fminf(fabsf(b), kSatScaled)));
+            const uint32_t signs = __byte_perm(as_u32(a), as_u32(b), 0x7430);
+            w = (signs & 0x80008000u) | __byte_perm(ma, mb, 0x5410);
         } else {
-            ca = f16c_encode(a);
-            cb = f16c_encode(b);
+            w = __byte_perm(f16c_encode(a), f16c_encode(b), 0x5410);
         }
-        *reinterpret_cast<uint32_t*>(p) = __byte_perm(ca, cb, 0x5410);
+        *reinterpret_cast<uint32_t*>(p) = w;
     }
 };
 
