@@ -151,15 +151,18 @@ __device__ __forceinline__ void pair_step(const StepArgs& a, const uint32_t tile
     static_for<0, Q>([&](auto qc) {
         constexpr int q = qc.value;
         constexpr int sx = -L::c(q, 0), sy = -L::c(q, 1), sz = -L::c(q, 2);
-        const int32_t o = own + dy[sy + 1] + dz[sz + 1] + (int32_t)(T * q);  // source row at x_A
+        // the source row at x_A: one 64-bit address per row (shared by its directions, whose q*T
+        // are immediate offsets) and one per x edge
+        const S* row = fin + (own + dy[sy + 1] + dz[sz + 1]);
+        constexpr int32_t qT = (int32_t)(T * q);
         if constexpr (sx == 0) {
-            W::ld(fin + o, fa[q], fb[q]);
+            W::ld(row + qT, fa[q], fb[q]);
         } else if constexpr (sx < 0) {
-            fa[q] = ld(fin + (o + dxm));
-            fb[q] = ld(fin + o);
+            fa[q] = ld(row + dxm + qT);
+            fb[q] = ld(row + qT);
         } else {
-            fa[q] = ld(fin + (o + 1));
-            fb[q] = ld(fin + (o + 1 + dxp));
+            fa[q] = ld(row + (qT + 1));
+            fb[q] = ld(row + dxp + (qT + 1));
         }
     });
 

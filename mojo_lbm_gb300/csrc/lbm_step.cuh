@@ -394,7 +394,25 @@ __device__ __forceinline__ void collide(float (&f)[L::Q], float tau, const StepA
             });
         }
     }
-    if constexpr (COLL == LBM_SRT) {
+    if constexpr (COLL == LBM_SRT && LES == kLesLearned) {
+        // SRT after the learned closure.  Its kernels are held to a tolerance (the network is
+        // BF16), so the relaxation takes the multiply-add form f' = (1 - w) f + w f_eq, with the
+        // equilibria of each opposite pair from one e.u: w f_eq(q, q+1) = w_q (a0 + 4.5 r0 (e.u)^2)
+        // +- 3 w_q r0 (e.u), a0 = w (rho (1 - 1.5 u.u) - ddf), r0 = w rho
+        // (src/lbm/kernels/utils/equilibrium.mojo:10-39, ops/collisions/collision.mojo:12-46).
+        const float om = 1.f / tau_local, om1 = 1.f - om;
+        const float a0 = om * (rho * (1.f - 1.5f * uu) - (ddf ? 1.f : 0.f)), r0 = om * rho;
+        f[0] = om1 * f[0] + wf<L>(0) * a0;
+        static_for<1, Q, 2>([&](auto qc) {
+            constexpr int q = qc.value;
+            constexpr float w = wf<L>(q);
+            const float eu = edot<L>(u, q);
+            const float c3 = (3.f * w) * r0;
+            const float base = ((4.5f * w) * r0) * (eu * eu) + w * a0;
+            f[q] = om1 * f[q] + (base + c3 * eu);
+            f[q + 1] = om1 * f[q + 1] + (base - c3 * eu);
+        });
+    } else if constexpr (COLL == LBM_SRT) {
         // SRT (src/lbm/kernels/ops/collisions/collision.mojo:12-46)
         float inv_tau;
         if constexpr (LES) inv_tau = 1.f / tau_local;
