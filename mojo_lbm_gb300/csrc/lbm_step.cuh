@@ -218,17 +218,51 @@ __device__ __forceinline__ void collide(float (&f)[L::Q], float tau, const StepA
     constexpr int Q = L::Q, D = L::D;
     const bool ddf = a.ddf != 0;
     float rho = 0.f;
-    static_for<0, Q>([&](auto qc) { rho += f[qc.value]; });
-    if (ddf) rho += 1.f;
     float mom[3] = {0.f, 0.f, 0.f};
-    static_for<0, Q>([&](auto qc) {
-        constexpr int q = qc.value;
+    [[maybe_unused]] float Praw[L::NS];  // learned closure: the raw second moment of f
+    if constexpr (LES == kLesLearned) {
+        // The learned-closure kernels are held to a tolerance (the network is BF16): the moments
+        // come from the sums and differences of opposite pairs (q, q+1), c_{q+1} = -c_q, as in the
+        // fast arithmetic (lbm_fast.cuh), in place of the reference's sums over q one by one.
+        constexpr int NP = (Q - 1) / 2;
+        float ps[NP], pd[NP];
+        static_for<0, NP>([&](auto pc) {
+            constexpr int p = pc.value, q = 2 * p + 1;
+            ps[p] = f[q] + f[q + 1];
+            pd[p] = f[q] - f[q + 1];
+        });
+        rho = f[0];
+        static_for<0, NP>([&](auto pc) { rho += ps[pc.value]; });
         static_for<0, D>([&](auto dc) {
             constexpr int d = dc.value;
-            if constexpr (L::c(q, d) > 0) mom[d] += f[q];
-            else if constexpr (L::c(q, d) < 0) mom[d] -= f[q];
+            static_for<0, NP>([&](auto pc) {
+                constexpr int p = pc.value, q = 2 * p + 1;
+                if constexpr (L::c(q, d) > 0) mom[d] += pd[p];
+                else if constexpr (L::c(q, d) < 0) mom[d] -= pd[p];
+            });
         });
-    });
+        static_for<0, L::NS>([&](auto nc) {
+            constexpr int n = nc.value;
+            Praw[n] = 0.f;
+            static_for<0, NP>([&](auto pc) {
+                constexpr int p = pc.value, q = 2 * p + 1;
+                constexpr int cc = L::c(q, sa<L>(n)) * L::c(q, sb<L>(n));
+                if constexpr (cc > 0) Praw[n] += ps[p];
+                else if constexpr (cc < 0) Praw[n] -= ps[p];
+            });
+        });
+    } else {
+        static_for<0, Q>([&](auto qc) { rho += f[qc.value]; });
+        static_for<0, Q>([&](auto qc) {
+            constexpr int q = qc.value;
+            static_for<0, D>([&](auto dc) {
+                constexpr int d = dc.value;
+                if constexpr (L::c(q, d) > 0) mom[d] += f[q];
+                else if constexpr (L::c(q, d) < 0) mom[d] -= f[q];
+            });
+        });
+    }
+    if (ddf) rho += 1.f;
     float u[3] = {0.f, 0.f, 0.f};
     // A cell with zero momentum (a fluid at rest) takes the signed zeros the divisions would give
     // (rho finite and not zero) without dividing: a zero numerator sends the IEEE division to its
@@ -271,15 +305,7 @@ __device__ __forceinline__ void collide(float (&f)[L::Q], float tau, const StepA
             // rho u_a u_b + cs^2 rho delta_ab on these lattices (cs^2 (rho - 1) delta_ab for the
             // DDF-shifted populations): algebraically equal, without f_eq per direction.  The
             // learned-closure kernels are held to a tolerance, not to bit parity.
-            static_for<0, Q>([&](auto qc) {
-                constexpr int q = qc.value;
-                static_for<0, L::NS>([&](auto nc) {
-                    constexpr int n = nc.value;
-                    constexpr int cc = L::c(q, sa<L>(n)) * L::c(q, sb<L>(n));
-                    if constexpr (cc > 0) P[n] += f[q];
-                    else if constexpr (cc < 0) P[n] -= f[q];
-                });
-            });
+            static_for<0, L::NS>([&](auto nc) { P[nc.value] = Praw[nc.value]; });
             const float rho_cs2 = (ddf ? rho - 1.f : rho) * (float)(1.0 / 3.0);
             static_for<0, L::NS>([&](auto nc) {
                 constexpr int n = nc.value, A = sa<L>(n), B = sb<L>(n);
