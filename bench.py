@@ -288,7 +288,7 @@ def run_ours(args, wl: dict):
         solver.set_block_threads(args.threads)
     kernel = args.kernel or wl.get("kernel", "auto")
     if kernel != "auto":
-        solver.set_kernel_path({"generic": 1, "tile": 2, "pair": 3, "staged": 4, "pairpf": 5}[kernel])
+        solver.set_kernel_path({"generic": 1, "tile": 2, "pair": 3, "staged": 4}[kernel])
     f_dtype = torch.int16 if cfg.use_float16c else torch.float32
     fa = torch.empty(N * Q, dtype=f_dtype, device=dev)
     fb = torch.empty_like(fa) if wl["method"] == "db" else fa
@@ -429,8 +429,7 @@ def run_ours(args, wl: dict):
                    "layout": "reference tiled layout (col-major tile, col-major tiler)", "tau": round(tau, 6),
                    "arithmetic": cfg.arithmetic,
                    "kernel": {1: "generic", 2: "block-per-tile", 3: "cell-pair block-per-tile",
-                              4: "staged block-per-tile (bulk async copies into shared memory)",
-                              5: "cell-pair block-per-tile, persistent, next tile prefetched"}[solver.kernel_path],
+                              4: "staged block-per-tile (bulk async copies into shared memory)"}[solver.kernel_path],
                    "timing": f"CUDA events around each of {len(reps)} replays of the K-step graph on the launching "
                              f"stream (at least {args.repeat_seconds:g} s in all); value from the median replay "
                              f"(min {min(reps) / K:.5f}, max {max(reps) / K:.5f} ms/step)",
@@ -708,7 +707,7 @@ def main(argv=None):
     ap.add_argument("--arithmetic", choices=["exact", "fast"], default=None,
                     help="the step's arithmetic: exact (the reference's operation order, bit-identical to the "
                          "float32 oracle) or fast (FMA rearranged, held to a float32 tolerance); default per workload")
-    ap.add_argument("--kernel", choices=["auto", "generic", "tile", "pair", "staged", "pairpf"], default=None,
+    ap.add_argument("--kernel", choices=["auto", "generic", "tile", "pair", "staged"], default=None,
                     help="step kernel: generic, block-per-tile, cell-pair block-per-tile (two cells per thread "
                          "along x) or staged block-per-tile (bulk async copies of each tile's neighbourhood into "
                          "shared memory); the last two double buffer only; default per workload")

@@ -152,9 +152,7 @@ lbm_status lbm_set_block_threads(lbm_handle* h, int32_t threads);
  * also needs the double-buffer method and tx >= 2, 4 = the staged block-per-tile kernel (persistent
  * CTAs; bulk asynchronous copies stage the next tile's pull neighbourhood in shared memory while
  * the current tile is stepped), which needs the double-buffer method and tile rows of a multiple of
- * 16 bytes (tx >= 8 Float16C, tx >= 4 float32) (LBM_EUNSUPPORTED otherwise), 5 = the cell-pair
- * kernel's persistent form, which loads each thread's pair of the next tile before it finishes the
- * current one (the requirements of 3).  A step whose
+ * 16 bytes (tx >= 8 Float16C, tx >= 4 float32) (LBM_EUNSUPPORTED otherwise).  A step whose
  * population buffers are not 8-byte (path 3) or 16-byte (path 4) aligned, or a handle with the
  * learned closure or fused links, runs the block-per-tile kernel (or its variant) instead.  The
  * automatic choice is the cell-pair kernel for double-buffer D2Q9 / D3Q19 configurations other than
@@ -163,7 +161,7 @@ lbm_status lbm_set_block_threads(lbm_handle* h, int32_t threads);
 lbm_status lbm_set_kernel_path(lbm_handle* h, int32_t path);
 
 /* The kernel lbm_*_step will use (aligned buffers): 1 generic, 2 block-per-tile, 3 cell-pair,
- * 4 staged, 5 cell-pair prefetching, -1 for a null handle. */
+ * 4 staged, -1 for a null handle. */
 int32_t lbm_kernel_path(const lbm_handle* h);
 
 /* Waits for the device and reports the errors the kernels raised on the device since the last

@@ -28,9 +28,6 @@ StepLaunch get_fast_tile_step_d3q27(int, int, int, int);
 StepLaunch get_pair_step_d2q9(int, int, int, int);
 StepLaunch get_pair_step_d3q19(int, int, int, int);
 StepLaunch get_pair_step_d3q27(int, int, int, int);
-StepLaunch get_pair_pf_step_d2q9(int, int, int, int);
-StepLaunch get_pair_pf_step_d3q19(int, int, int, int);
-StepLaunch get_pair_pf_step_d3q27(int, int, int, int);
 StepLaunch get_links_tile_step_d2q9(int, int, int, int);
 StepLaunch get_staged_step_d2q9(int, int, int, int);
 StepLaunch get_staged_step_d3q19(int, int, int, int);
@@ -116,7 +113,6 @@ struct lbm_handle {
     StepLaunch step_learned;  // block-per-tile kernel with the learned closure (LES handles), or null
     StepLaunch step_pair;  // cell-pair block-per-tile kernel (double buffer, tx >= 2), or null
     int pair_auto;         // the automatic choice takes the cell-pair kernel
-    StepLaunch step_pair_pf;  // its prefetching persistent form (kernel path 5), or null
     StepLaunch step_links;    // block-per-tile kernel with fused links (double buffer), or null
     StepLaunch step_staged;   // staged block-per-tile kernel (double buffer, 16-byte tile rows), or null
     int path;              // 0 auto, 1 generic only, 2 block-per-tile only, 3 cell-pair, 4 staged
@@ -226,8 +222,8 @@ bool use_staged(const lbm_handle* h) {
 // double-buffer D2Q9 / D3Q19 configurations other than KBC (whose larger register demand halves the
 // pair kernel's occupancy).
 bool use_pair(const lbm_handle* h) {
-    return (h->path == 3 || h->path == 5 || (h->path == 0 && h->pair_auto)) && h->step_pair != nullptr &&
-           !h->closure_on && !h->link_table;
+    return (h->path == 3 || (h->path == 0 && h->pair_auto)) && h->step_pair != nullptr && !h->closure_on &&
+           !h->link_table;
 }
 
 // The kernel the next step with these arguments runs.  The cell-pair kernel moves 8-byte
@@ -239,7 +235,8 @@ StepLaunch step_fn(const lbm_handle* h, const StepArgs& a) {
     if (h->link_table) return h->step_links;
     const uintptr_t al = reinterpret_cast<uintptr_t>(a.f_in) | reinterpret_cast<uintptr_t>(a.f_out);
     if (use_staged(h) && (al & 15u) == 0u) return h->step_staged;  // bulk copies: 16-byte aligned rows
-    if (use_pair(h) && (al & 7u) == 0u) return h->path == 5 ? h->step_pair_pf : h->step_pair;
+    if (use_pair(h) && ((reinterpret_cast<uintptr_t>(a.f_in) | reinterpret_cast<uintptr_t>(a.f_out)) & 7u) == 0u)
+        return h->step_pair;
     return h->step_tile;
 }
 
@@ -414,10 +411,6 @@ lbm_status lbm_create(const lbm_config_t* cfg, const lbm_grid_t* grid, lbm_handl
                    : grid->lattice == LBM_D3Q19 ? get_staged_step_d3q19(f16, co, les, fast)
                                                 : get_staged_step_d3q27(f16, co, les, fast);
     h->pair_auto = h->step_pair != nullptr && co != LBM_KBC && grid->lattice != LBM_D3Q27;
-    h->step_pair_pf = !h->step_pair ? nullptr
-                    : grid->lattice == LBM_D2Q9 ? get_pair_pf_step_d2q9(f16, co, les, fast)
-                    : grid->lattice == LBM_D3Q19 ? get_pair_pf_step_d3q19(f16, co, les, fast)
-                                                 : get_pair_pf_step_d3q27(f16, co, les, fast);
     h->path = 0;
     h->ntiles = h->lay.ncells / h->lay.T;
     h->mx = (uint32_t)grid->tx - 1u;
@@ -581,12 +574,8 @@ lbm_status lbm_set_block_threads(lbm_handle* h, int32_t threads) {
 
 lbm_status lbm_set_kernel_path(lbm_handle* h, int32_t path) {
     if (check_handle(h)) return LBM_EINVAL;
-    if (path < 0 || path > 5)
-        return fail(LBM_EINVAL, "path must be 0 (auto), 1 (generic), 2 (block-per-tile), 3 (cell-pair), 4 (staged) "
-                                "or 5 (cell-pair, prefetching)");
-    if (path == 5 && !h->step_pair_pf)
-        return fail(LBM_EUNSUPPORTED, "the cell-pair kernel needs the double-buffer method, 256-cell power-of-two "
-                                      "tiles with tx >= 2 and Q*N < 2^31");
+    if (path < 0 || path > 4)
+        return fail(LBM_EINVAL, "path must be 0 (auto), 1 (generic), 2 (block-per-tile), 3 (cell-pair) or 4 (staged)");
     if (path == 4 && !h->step_staged)
         return fail(LBM_EUNSUPPORTED, "the staged kernel needs the double-buffer method, 256-cell power-of-two tiles "
                                       "whose rows are multiples of 16 bytes (tx >= 8 Float16C, tx >= 4 float32) and "
@@ -605,7 +594,7 @@ lbm_status lbm_set_kernel_path(lbm_handle* h, int32_t path) {
 }
 
 int32_t lbm_kernel_path(const lbm_handle* h) {
-    return h ? (use_tile(h) ? (use_staged(h) ? 4 : use_pair(h) ? (h->path == 5 ? 5 : 3) : 2) : 1) : -1;
+    return h ? (use_tile(h) ? (use_staged(h) ? 4 : use_pair(h) ? 3 : 2) : 1) : -1;
 }
 
 lbm_status lbm_device_status(lbm_handle* h) {
@@ -680,7 +669,7 @@ lbm_status lbm_run(lbm_handle* h, void* f_a, void* f_b, float* bc, const uint8_t
     if (n_steps >= chunk) {
         uint32_t tau_bits;
         std::memcpy(&tau_bits, &tau, 4);
-        const GraphKey key{f_a, f_b, bc, flags, tau_bits, (int)(first_step % 2), chunk, use_tile(h) ? (use_staged(h) ? 4 : use_pair(h) ? (h->path == 5 ? 5 : 3) : 2) : 1};
+        const GraphKey key{f_a, f_b, bc, flags, tau_bits, (int)(first_step % 2), chunk, use_tile(h) ? (use_staged(h) ? 4 : use_pair(h) ? 3 : 2) : 1};
         auto it = h->graphs.find(key);
         if (it == h->graphs.end()) {
             cudaGraph_t g = nullptr;

@@ -415,14 +415,12 @@ __device__ __forceinline__ void pair_finish(const StepArgs& a, const uint32_t ti
     }
 }
 
-// Resident CTAs per SM: the next tile's words and the current pair's populations are live
-// together, so Float16C takes 128 registers (4 CTAs) and float32 168 (3 CTAs) without spilling.
 #ifndef LBM_PAIR_PF_MIN_BLOCKS
-#define LBM_PAIR_PF_MIN_BLOCKS 4
+#define LBM_PAIR_PF_MIN_BLOCKS 5
 #endif
 
 template <class L, bool F16C, int COLL, int LES, bool FAST>
-__global__ void __launch_bounds__(kPairThreads, ((COLL == LBM_KBC || L::Q == 27 || !F16C) ? 3 : LBM_PAIR_PF_MIN_BLOCKS))
+__global__ void __launch_bounds__(kPairThreads, ((COLL == LBM_KBC || L::Q == 27) ? 3 : LBM_PAIR_PF_MIN_BLOCKS))
     step_kernel_pair_pf(const StepArgs a) {
     static_assert(LES != kLesLearned, "the learned closure runs in step_kernel_learned");
     const uint32_t ntiles = a.lay.ncells / kTileCells, G = gridDim.x, t = threadIdx.x;

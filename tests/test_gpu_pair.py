@@ -29,14 +29,11 @@ CASES = list(itertools.product(["D2Q9", "D3Q19", "D3Q27"], ["fp32", "f16c"], ["S
                                [False, True], ["mixed", "ldc"]))
 
 
-@pytest.mark.parametrize("path", [3, 5], ids=["pair", "prefetch"])
 @pytest.mark.parametrize("lat,store,coll,les,case", CASES, ids=["-".join(map(str, c)) for c in CASES])
-def test_pair_step_parity(lat, store, coll, les, case, path):
-    """Path 3, and path 5 (its persistent form that loads the next tile's pair before finishing
-    the current one)."""
+def test_pair_step_parity(lat, store, coll, les, case):
     shape, tile = TILE_SHAPES[lat]
     grid, cfg, flags, bc, f0, tau = step_case(lat, "db", store, coll, les, case, shape, tile)
-    got, ref, bc_gpu, bc_ref = run_both(grid, cfg, flags, bc, f0, tau, 6, path=path)
+    got, ref, bc_gpu, bc_ref = run_both(grid, cfg, flags, bc, f0, tau, 6, path=3)
     assert_close(got, ref, cfg, f"pair {lat}/{store}/{coll}/LES={les}/{case}")
     if case == "mixed":
         assert np.array_equal(bc_gpu.view(np.uint32), bc_ref.view(np.uint32))
@@ -49,10 +46,9 @@ PAIR_TILES = {"D2Q9": ((256, 256, 1), [(256, 1, 1), (32, 8, 1), (16, 16, 1), (4,
 PAIR_TILE_CASES = [(lat, t, f16) for lat, (_, ts) in PAIR_TILES.items() for t in ts for f16 in (False, True)]
 
 
-@pytest.mark.parametrize("path", [3, 5], ids=["pair", "prefetch"])
 @pytest.mark.parametrize("lat,tile,f16", PAIR_TILE_CASES,
                          ids=[f"{c[0]}-{'x'.join(map(str, c[1]))}-{'f16c' if c[2] else 'fp32'}" for c in PAIR_TILE_CASES])
-def test_pair_sparse_flags(lat, tile, f16, path):
+def test_pair_sparse_flags(lat, tile, f16):
     """Isolated flags of every kind in a periodic grid: pairs whose box is flagged next to pairs
     whose box is clear in the same warp, a SOLID or EXCLUDE cell beside an active one (half-pair
     stores), tile-edge x neighbours (tx = 2: every pair touches both x edges)."""
@@ -63,7 +59,7 @@ def test_pair_sparse_flags(lat, tile, f16, path):
     flags, bc = mixed_flags(grid, rng)
     flags[rng.random(flags.size) >= 0.004] = 0
     f0 = initial_f(grid, cfg, rng)
-    got, ref, bc_gpu, bc_ref = run_both(grid, cfg, flags, bc, f0, 0.8, 4, path=path)
+    got, ref, bc_gpu, bc_ref = run_both(grid, cfg, flags, bc, f0, 0.8, 4, path=3)
     assert_close(got, ref, cfg, f"pair sparse flags, tile {tile}")
     assert np.array_equal(bc_gpu.view(np.uint32), bc_ref.view(np.uint32))
 
@@ -110,11 +106,10 @@ def test_pair_fast_equals_tile_fast(lat, store, coll, les):
     grid, cfg, flags, bc, f0, tau = step_case(lat, "db", store, coll, les, "mixed", shape, tile)
     cfg.arithmetic = "fast"
     a, bca = _run(grid, cfg, flags, bc, f0, tau, 66, 2)
+    b, bcb = _run(grid, cfg, flags, bc, f0, tau, 66, 3)
     word = np.uint16 if a.dtype == np.uint16 else np.uint32
-    for path in (3, 5):
-        b, bcb = _run(grid, cfg, flags, bc, f0, tau, 66, path)
-        assert np.array_equal(a.view(word), b.view(word)), path
-        assert np.array_equal(bca.view(np.uint32), bcb.view(np.uint32)), path
+    assert np.array_equal(a.view(word), b.view(word))
+    assert np.array_equal(bca.view(np.uint32), bcb.view(np.uint32))
 
 
 @pytest.mark.parametrize("store", ["fp32", "f16c"])
