@@ -232,242 +232,6 @@ __device__ __forceinline__ void pair_step(const StepArgs& a, const uint32_t tile
     }
 }
 
-// ---------------------------------------------------------------------------------------------
-// The prefetching form of the pair step (kernel path 5): a persistent CTA walks tiles, and each
-// thread issues the loads of its pair in the next tile before it decodes, collides and stores the
-// current one, so the pull loads of one tile are in flight while the previous tile is computed.
-// The loaded words wait in registers as loaded (Float16C codes sign-extended, not decoded).
-// ---------------------------------------------------------------------------------------------
-
-// A pair's pulled populations as loaded: per direction the aligned pair's word (c.x = 0: both
-// halves in a for Float16C, a and b for float32) or the two cells' values, and the tile's mask byte.
-template <class L, bool F16C>
-struct PairRaw {
-    using R = std::conditional_t<F16C, uint32_t, float>;
-    R a[L::Q], b[L::Q];
-    uint32_t near;
-};
-
-template <class L, bool F16C>
-__device__ __forceinline__ void pair_load(const StepArgs& a, const uint32_t tile, const uint32_t t,
-                                          PairRaw<L, F16C>& r) {
-    using S = typename Pop<F16C>::T;
-    constexpr int Q = L::Q, D = L::D;
-    constexpr uint32_t T = kTileCells;
-    const uint32_t tA = 2u * t;
-    const uint32_t byz = a.lay.d_ntx.div(tile);
-    const uint32_t bx = tile - byz * (uint32_t)a.lay.ntx;
-    const uint32_t bz = a.lay.d_nty.div(byz);
-    const uint32_t by = byz - bz * (uint32_t)a.lay.nty;
-    const uint32_t lxA = tA & a.mx, ly = (tA >> a.shx) & a.my, lz = tA >> a.shxy;
-    const int32_t TQ = (int32_t)(T * Q);
-    int32_t dxm, dxp, dy[3], dz[3];
-    pair_deltas<D>(a, bx, by, bz, lxA, ly, lz, TQ, dxm, dxp, dy, dz);
-    const int32_t own = (int32_t)tA + TQ * (int32_t)tile;
-    const S* fin = (const S*)a.f_in;
-    auto raw = [](const S* p) -> typename PairRaw<L, F16C>::R {
-        if constexpr (F16C) return (uint32_t)(int32_t)__ldg(reinterpret_cast<const int16_t*>(p));
-        else return __ldg(p);
-    };
-    r.near = (uint32_t)__ldg(a.tile_near + tile);
-    static_for<0, Q>([&](auto qc) {
-        constexpr int q = qc.value;
-        constexpr int sx = -L::c(q, 0), sy = -L::c(q, 1), sz = -L::c(q, 2);
-        const S* row = fin + (own + dy[sy + 1] + dz[sz + 1]);
-        constexpr int32_t qT = (int32_t)(T * q);
-        if constexpr (sx == 0) {
-            if constexpr (F16C) {
-                r.a[q] = __ldg(reinterpret_cast<const uint32_t*>(row + qT));
-            } else {
-                const float2 v = __ldg(reinterpret_cast<const float2*>(row + qT));
-                r.a[q] = v.x;
-                r.b[q] = v.y;
-            }
-        } else if constexpr (sx < 0) {
-            r.a[q] = raw(row + dxm + qT);
-            r.b[q] = raw(row + qT);
-        } else {
-            r.a[q] = raw(row + (qT + 1));
-            r.b[q] = raw(row + dxp + (qT + 1));
-        }
-    });
-}
-
-// The rest of pair_step on the loaded words of tile `tile`: decode, boundaries, collision, store.
-template <class L, bool F16C, int COLL, int LES, bool FAST>
-__device__ __forceinline__ void pair_finish(const StepArgs& a, const uint32_t tile, const uint32_t t,
-                                            const PairRaw<L, F16C>& r) {
-    using P = Pop<F16C>;
-    using S = typename P::T;
-    constexpr int Q = L::Q, D = L::D, K = D + 1;
-    constexpr uint32_t T = kTileCells;
-    constexpr bool SCALED = FAST && F16C && !LES && COLL != LBM_KBC;
-    using W = PairWord<F16C, SCALED>;
-    auto ld = [](const S* p) -> float {
-        if constexpr (SCALED) return P::ld_scaled(p);
-        else return P::ld(p);
-    };
-    auto st = [](S* p, float v) {
-        if constexpr (SCALED) P::st_scaled(p, v);
-        else P::st(p, v);
-    };
-    auto dec = [](uint32_t code_sx) -> float {
-        if constexpr (SCALED) return f16c_decode_scaled_sx((int32_t)code_sx);
-        else return f16c_decode_sx((int32_t)code_sx);
-    };
-
-    float fa[Q], fb[Q];
-    static_for<0, Q>([&](auto qc) {
-        constexpr int q = qc.value;
-        if constexpr (!F16C) {
-            fa[q] = r.a[q];
-            fb[q] = r.b[q];
-        } else if constexpr (L::c(q, 0) == 0) {
-            const uint32_t w = r.a[q];
-            fa[q] = dec((uint32_t)((int32_t)(w << 16) >> 16));
-            fb[q] = dec((uint32_t)((int32_t)w >> 16));
-        } else {
-            fa[q] = dec(r.a[q]);
-            fb[q] = dec(r.b[q]);
-        }
-    });
-
-    const uint32_t tA = 2u * t;
-    const uint32_t nA = tA + T * tile;
-    const uint32_t mask = r.near;
-    const uint32_t box = tA >> 5;
-    const bool clean = __all_sync(0xffffffffu, ((mask >> ((t >> 5) * 2u)) & 3u) == 0u);
-    const bool flagged = !clean && ((mask >> box) & 1u);
-    uint8_t flagA = 0, flagB = 0;
-    bool actA = true, actB = true;
-    if (flagged) {
-        flagA = __ldg(a.flags + nA);
-        flagB = __ldg(a.flags + nA + 1u);
-        actA = !((flagA & 0x0F) == LBM_FLAG_SOLID || (flagA & LBM_FLAG_EXCLUDE));
-        actB = !((flagB & 0x0F) == LBM_FLAG_SOLID || (flagB & LBM_FLAG_EXCLUDE));
-        if (!actA && !actB) return;
-    }
-    const int32_t TQ = (int32_t)(T * Q);
-    const int32_t own = (int32_t)tA + TQ * (int32_t)tile;
-    const S* fin = (const S*)a.f_in;
-    S* fout = (S*)a.f_out;
-    if (flagged) {
-        const uint32_t byz = a.lay.d_ntx.div(tile);
-        const uint32_t bx = tile - byz * (uint32_t)a.lay.ntx;
-        const uint32_t bz = a.lay.d_nty.div(byz);
-        const uint32_t by = byz - bz * (uint32_t)a.lay.nty;
-        const uint32_t lxA = tA & a.mx, ly = (tA >> a.shx) & a.my, lz = tA >> a.shxy;
-        const uint4 m = __ldg(reinterpret_cast<const uint4*>(a.cell_masks + nA));
-        if (m.x)
-            static_for<1, Q>([&](auto qc) {
-                constexpr int q = qc.value;
-                if ((m.x >> q) & 1u) fa[q] = ld(fin + own + (int32_t)(T * opp<L>(q)));
-            });
-        if (m.z)
-            static_for<1, Q>([&](auto qc) {
-                constexpr int q = qc.value;
-                if ((m.z >> q) & 1u) fb[q] = ld(fin + own + 1 + (int32_t)(T * opp<L>(q)));
-            });
-        if (a.moving && (m.y | m.w)) {
-            auto wall = [&](float (&f)[Q], uint32_t nib, uint32_t tc) {
-                int32_t dc[3][3], dp[3][3];
-                tile_deltas<D>(a, bx, by, bz, tc & a.mx, ly, lz, TQ, dc, dp);
-                const uint32_t n = tc + T * tile;
-                moving_wall<L, SCALED>(f, nib, a.bc, T, [&](auto qc) -> uint64_t {
-                    constexpr int q = decltype(qc)::value;
-                    constexpr int sx = -L::c(q, 0), sy = -L::c(q, 1), sz = -L::c(q, 2);
-                    const uint32_t mm = (uint32_t)((int32_t)n + dc[0][sx + 1] + dc[1][sy + 1] + dc[2][sz + 1]);
-                    const uint32_t mt = mm / T;
-                    return (uint64_t)(mm - mt * T) + (uint64_t)T * K * mt;
-                });
-            };
-            if (m.y) wall(fa, m.y, tA);
-            if (m.w) wall(fb, m.w, tA + 1u);
-        }
-        if (a.eqbc) {
-            const int32_t gx = (int32_t)(bx * (uint32_t)a.lay.tx + lxA), gy = (int32_t)(by * (uint32_t)a.lay.ty + ly),
-                          gz = (int32_t)(bz * (uint32_t)a.lay.tz + lz);
-            auto eq = [&](float (&f)[Q], uint32_t tc, int32_t x) {
-                if constexpr (SCALED) static_for<0, Q>([&](auto qc) { f[qc.value] *= 0x1p112f; });
-                equilibrium_bc<L>(f, a.bc, tc + (uint64_t)T * K * tile, T, x, gy, gz, a.lay, a.ddf != 0);
-                if constexpr (SCALED) static_for<0, Q>([&](auto qc) { f[qc.value] *= 0x1p-112f; });
-            };
-            if ((flagA & 0x0F) == LBM_FLAG_EQUILIBRIUM) eq(fa, tA, gx);
-            if ((flagB & 0x0F) == LBM_FLAG_EQUILIBRIUM) eq(fb, tA + 1u, gx + 1);
-        }
-    }
-    float* bcA = a.bc + (tA + (uint64_t)T * K * tile);
-    if (actA) {
-        if constexpr (FAST) collide_fast<L, COLL, LES, SCALED>(fa, a, bcA, T, flagA);
-        else collide<L, COLL, LES>(fa, a.tau, a, bcA, T, flagA);
-    }
-    if (actB) {
-        if constexpr (FAST) collide_fast<L, COLL, LES, SCALED>(fb, a, bcA + 1, T, flagB);
-        else collide<L, COLL, LES>(fb, a.tau, a, bcA + 1, T, flagB);
-    }
-    S* po = fout + own;
-    if (actA && actB) {
-        static_for<0, Q>([&](auto qc) { W::st(po + (int32_t)(T * qc.value), fa[qc.value], fb[qc.value]); });
-    } else if (actA) {
-        static_for<0, Q>([&](auto qc) { st(po + (int32_t)(T * qc.value), fa[qc.value]); });
-    } else {
-        static_for<0, Q>([&](auto qc) { st(po + 1 + (int32_t)(T * qc.value), fb[qc.value]); });
-    }
-}
-
-#ifndef LBM_PAIR_PF_MIN_BLOCKS
-#define LBM_PAIR_PF_MIN_BLOCKS 5
-#endif
-
-template <class L, bool F16C, int COLL, int LES, bool FAST>
-__global__ void __launch_bounds__(kPairThreads, ((COLL == LBM_KBC || L::Q == 27) ? 3 : LBM_PAIR_PF_MIN_BLOCKS))
-    step_kernel_pair_pf(const StepArgs a) {
-    static_assert(LES != kLesLearned, "the learned closure runs in step_kernel_learned");
-    const uint32_t ntiles = a.lay.ncells / kTileCells, G = gridDim.x, t = threadIdx.x;
-    uint32_t tile = blockIdx.x;
-    if (tile >= ntiles) return;
-    PairRaw<L, F16C> r0, r1;
-    pair_load<L, F16C>(a, tile, t, r0);
-    for (;;) {  // two tiles per turn, so the two register sets alternate without copies
-        const uint32_t t1 = tile + G;
-        if (t1 < ntiles) pair_load<L, F16C>(a, t1, t, r1);
-        pair_finish<L, F16C, COLL, LES, FAST>(a, tile, t, r0);
-        if (t1 >= ntiles) break;
-        const uint32_t t2 = t1 + G;
-        if (t2 < ntiles) pair_load<L, F16C>(a, t2, t, r0);
-        pair_finish<L, F16C, COLL, LES, FAST>(a, t1, t, r1);
-        if (t2 >= ntiles) break;
-        tile = t2;
-    }
-}
-
-template <class L, bool F16C, int COLL, int LES, bool FAST>
-cudaError_t launch_step_pair_pf_impl(const StepArgs& a, cudaStream_t s) {
-    auto kernel = step_kernel_pair_pf<L, F16C, COLL, LES, FAST>;
-    static int per_sm = 0, sms = 0;
-    if (per_sm == 0) {
-        int dev = 0;
-        cudaError_t e = cudaGetDevice(&dev);
-        if (e == cudaSuccess) e = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-        if (e == cudaSuccess) e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kernel, (int)kPairThreads, 0);
-        if (e != cudaSuccess) return e;
-        if (per_sm < 1) per_sm = 1;
-    }
-    const uint32_t ntiles = a.lay.ncells / kTileCells;
-    kernel<<<min(ntiles, (uint32_t)(sms * per_sm)), kPairThreads, 0, s>>>(a);
-    return cudaGetLastError();
-}
-template <class L, int METHOD, bool F16C, int COLL, int LES>
-cudaError_t launch_step_pair_pf(const StepArgs& a, int, cudaStream_t s) {
-    static_assert(METHOD == LBM_DOUBLE_BUFFER, "the cell-pair kernel is double-buffer only");
-    return launch_step_pair_pf_impl<L, F16C, COLL, LES, false>(a, s);
-}
-template <class L, int METHOD, bool F16C, int COLL, int LES>
-cudaError_t launch_step_pair_pf_fast(const StepArgs& a, int, cudaStream_t s) {
-    static_assert(METHOD == LBM_DOUBLE_BUFFER, "the cell-pair kernel is double-buffer only");
-    return launch_step_pair_pf_impl<L, F16C, COLL, LES, true>(a, s);
-}
-
 // Resident CTAs (of 128 threads) per SM the pair kernels are built for: the populations of two
 // cells stay in registers across both collisions, so the budget is wider than the per-cell
 // kernel's.  Float16C and float32 7 (72 registers; measured against 6, 8 and 10 on the Float16C

@@ -9,12 +9,3 @@ StepLaunch get_pair_step_d3q19(int f16c, int coll, int les, int fast) {
     return (fast ? fastt : exact)[db_index(f16c, coll, les)];
 }
 }  // namespace lbm
-
-namespace lbm {
-// The prefetching persistent form (kernel path 5), exact and fast arithmetic.
-StepLaunch get_pair_pf_step_d3q19(int f16c, int coll, int les, int fast) {
-    static const StepLaunch exact[16] = LBM_DB_TABLE(launch_step_pair_pf, D3Q19);
-    static const StepLaunch fastt[16] = LBM_DB_TABLE(launch_step_pair_pf_fast, D3Q19);
-    return (fast ? fastt : exact)[db_index(f16c, coll, les)];
-}
-}  // namespace lbm
