@@ -97,8 +97,15 @@ __device__ __forceinline__ void pair_deltas(const StepArgs& a, uint32_t bx, uint
     }
 }
 
-template <class L, bool F16C, int COLL, int LES, bool FAST>
-__device__ __forceinline__ void pair_step(const StepArgs& a, const uint32_t tile, const uint32_t t) {
+// The two cells of one thread.  GENERAL = false is the all-fluid form (the warp's two boxes hold
+// no flag and pull from no flagged cell): no flag is read, both cells are active and the code is
+// straight-line from the loads to the stores, so the scheduler interleaves the two collisions.
+// GENERAL = true reads the flags of the cells whose box bit is set and handles them as tile_step
+// does.
+template <class L, bool F16C, int COLL, int LES, bool FAST, bool GENERAL>
+__device__ __forceinline__ void pair_cells(const StepArgs& a, const uint32_t tile, const uint32_t t,
+                                           const uint32_t mask, const uint32_t bx, const uint32_t by,
+                                           const uint32_t bz) {
     using P = Pop<F16C>;
     using S = typename P::T;
     constexpr int Q = L::Q, D = L::D, K = D + 1;
@@ -116,27 +123,29 @@ __device__ __forceinline__ void pair_step(const StepArgs& a, const uint32_t tile
 
     const uint32_t tA = 2u * t;         // cell A; B = tA + 1
     const uint32_t nA = tA + T * tile;  // flag offset of A
-    const uint32_t byz = a.lay.d_ntx.div(tile);
-    const uint32_t bx = tile - byz * (uint32_t)a.lay.ntx;
-    const uint32_t bz = a.lay.d_nty.div(byz);
-    const uint32_t by = byz - bz * (uint32_t)a.lay.nty;
-
-    // ---- the warp's two boxes (cells 64w .. 64w + 63) all plain FLUID with FLUID neighbours?
-    const uint32_t mask = (uint32_t)__ldg(a.tile_near + tile);
-    const uint32_t box = tA >> 5;  // the pair's box (both cells)
-    const bool clean = __all_sync(0xffffffffu, ((mask >> ((t >> 5) * 2u)) & 3u) == 0u);
-    const bool flagged = !clean && ((mask >> box) & 1u);
+    const bool flagged = GENERAL && ((mask >> (tA >> 5)) & 1u);  // the pair's box (both cells)
 
     uint8_t flagA = 0, flagB = 0;
     bool actA = true, actB = true;
+    // cell-solid masks of both cells (written for every cell of a flagged box): x, z the SOLID pull
+    // neighbours of A, B; y, w those with a moving-wall bc
+    uint4 m = make_uint4(0u, 0u, 0u, 0u);
     if (flagged) {
         flagA = __ldg(a.flags + nA);
         flagB = __ldg(a.flags + nA + 1u);
         // is_valid_thread (src/lbm/kernels/utils/checks.mojo:55-60), per cell
         actA = !((flagA & 0x0F) == LBM_FLAG_SOLID || (flagA & LBM_FLAG_EXCLUDE));
         actB = !((flagB & 0x0F) == LBM_FLAG_SOLID || (flagB & LBM_FLAG_EXCLUDE));
-        if (!actA && !actB) return;
+        m = __ldg(reinterpret_cast<const uint4*>(a.cell_masks + nA));
     }
+    // The directions that any cell of the warp bounces back or takes a moving wall in (all 32 lanes
+    // are converged here): a direction no lane needs is skipped by the whole warp.
+    uint32_t bb_any = 0u, mw_any = 0u;
+    if constexpr (GENERAL) {
+        bb_any = __reduce_or_sync(0xffffffffu, m.x | m.z);
+        mw_any = __reduce_or_sync(0xffffffffu, m.y | m.w);
+    }
+    if (flagged && !actA && !actB) return;
 
     const uint32_t lxA = tA & a.mx, ly = (tA >> a.shx) & a.my, lz = tA >> a.shxy;
     const int32_t TQ = (int32_t)(T * Q);
@@ -166,33 +175,33 @@ __device__ __forceinline__ void pair_step(const StepArgs& a, const uint32_t tile
         }
     });
 
-    if (flagged) {
-        // ---- cell-solid masks of both cells (written for every cell of a flagged box)
-        const uint4 m = __ldg(reinterpret_cast<const uint4*>(a.cell_masks + nA));
-        // mid-grid bounce-back on a raw SOLID compare (ops/load_and_store.mojo:216)
-        if (m.x)
-            static_for<1, Q>([&](auto qc) {
-                constexpr int q = qc.value;
+    if (bb_any) {
+        // ---- mid-grid bounce-back on a raw SOLID compare (ops/load_and_store.mojo:216)
+        static_for<1, Q>([&](auto qc) {
+            constexpr int q = qc.value;
+            if ((bb_any >> q) & 1u) {
                 if ((m.x >> q) & 1u) fa[q] = ld(fin + own + (int32_t)(T * opp<L>(q)));
-            });
-        if (m.z)
-            static_for<1, Q>([&](auto qc) {
-                constexpr int q = qc.value;
                 if ((m.z >> q) & 1u) fb[q] = ld(fin + own + 1 + (int32_t)(T * opp<L>(q)));
-            });
-        if (a.moving && (m.y | m.w)) {
+            }
+        });
+    }
+    if (flagged) {
+        if (a.moving && mw_any) {
             // moving_wall_bc with the bc of each cell's SOLID pull neighbours
             auto wall = [&](float (&f)[Q], uint32_t nib, uint32_t tc) {
                 int32_t dc[3][3], dp[3][3];
                 tile_deltas<D>(a, bx, by, bz, tc & a.mx, ly, lz, TQ, dc, dp);
                 const uint32_t n = tc + T * tile;
-                moving_wall<L, SCALED>(f, nib, a.bc, T, [&](auto qc) -> uint64_t {
-                    constexpr int q = decltype(qc)::value;
-                    constexpr int sx = -L::c(q, 0), sy = -L::c(q, 1), sz = -L::c(q, 2);
-                    const uint32_t mm = (uint32_t)((int32_t)n + dc[0][sx + 1] + dc[1][sy + 1] + dc[2][sz + 1]);
-                    const uint32_t mt = mm / T;
-                    return (uint64_t)(mm - mt * T) + (uint64_t)T * K * mt;
-                });
+                moving_wall<L, SCALED>(
+                    f, nib, a.bc, T,
+                    [&](auto qc) -> uint64_t {
+                        constexpr int q = decltype(qc)::value;
+                        constexpr int sx = -L::c(q, 0), sy = -L::c(q, 1), sz = -L::c(q, 2);
+                        const uint32_t mm = (uint32_t)((int32_t)n + dc[0][sx + 1] + dc[1][sy + 1] + dc[2][sz + 1]);
+                        const uint32_t mt = mm / T;
+                        return (uint64_t)(mm - mt * T) + (uint64_t)T * K * mt;
+                    },
+                    mw_any);
             };
             if (m.y) wall(fa, m.y, tA);
             if (m.w) wall(fb, m.w, tA + 1u);
@@ -212,6 +221,18 @@ __device__ __forceinline__ void pair_step(const StepArgs& a, const uint32_t tile
 
     // ---- collide each cell
     float* bcA = a.bc + (tA + (uint64_t)T * K * tile);
+    S* po = fout + own;
+    if constexpr (!GENERAL) {
+        if constexpr (FAST) {
+            collide_fast<L, COLL, LES, SCALED>(fa, a, bcA, T, 0);
+            collide_fast<L, COLL, LES, SCALED>(fb, a, bcA + 1, T, 0);
+        } else {
+            collide<L, COLL, LES>(fa, a.tau, a, bcA, T, 0);
+            collide<L, COLL, LES>(fb, a.tau, a, bcA + 1, T, 0);
+        }
+        static_for<0, Q>([&](auto qc) { W::st(po + (int32_t)(T * qc.value), fa[qc.value], fb[qc.value]); });
+        return;
+    }
     if (actA) {
         if constexpr (FAST) collide_fast<L, COLL, LES, SCALED>(fa, a, bcA, T, flagA);
         else collide<L, COLL, LES>(fa, a.tau, a, bcA, T, flagA);
@@ -222,7 +243,6 @@ __device__ __forceinline__ void pair_step(const StepArgs& a, const uint32_t tile
     }
 
     // ---- store: one word per direction, or the active cell's half
-    S* po = fout + own;
     if (actA && actB) {
         static_for<0, Q>([&](auto qc) { W::st(po + (int32_t)(T * qc.value), fa[qc.value], fb[qc.value]); });
     } else if (actA) {
@@ -230,6 +250,20 @@ __device__ __forceinline__ void pair_step(const StepArgs& a, const uint32_t tile
     } else {
         static_for<0, Q>([&](auto qc) { st(po + 1 + (int32_t)(T * qc.value), fb[qc.value]); });
     }
+}
+
+template <class L, bool F16C, int COLL, int LES, bool FAST>
+__device__ __forceinline__ void pair_step(const StepArgs& a, const uint32_t tile, const uint32_t t) {
+    const uint32_t byz = a.lay.d_ntx.div(tile);
+    const uint32_t bx = tile - byz * (uint32_t)a.lay.ntx;
+    const uint32_t bz = a.lay.d_nty.div(byz);
+    const uint32_t by = byz - bz * (uint32_t)a.lay.nty;
+    // ---- the warp's two boxes (cells 64w .. 64w + 63) all plain FLUID with FLUID neighbours?
+    const uint32_t mask = (uint32_t)__ldg(a.tile_near + tile);
+    if (__all_sync(0xffffffffu, ((mask >> ((t >> 5) * 2u)) & 3u) == 0u))
+        pair_cells<L, F16C, COLL, LES, FAST, false>(a, tile, t, mask, bx, by, bz);
+    else
+        pair_cells<L, F16C, COLL, LES, FAST, true>(a, tile, t, mask, bx, by, bz);
 }
 
 // Resident CTAs (of 128 threads) per SM the pair kernels are built for: the populations of two

@@ -476,12 +476,15 @@ namespace lbm {
 // (enum) node, f_q += 6 w_q rho_w (c_q . u_w) with u_w, rho_w read at the solid node.
 // bc_base(q) returns the element offset of component 0 of the pull neighbour's bc.  SCALED: f holds
 // populations times 2^-112 (the fast build's scaled Float16C codes), and so does the added term.
+// warp_any: a superset of nib_solid that is the same in every lane (the warp's union), so that the
+// warp branches past the directions no lane needs.
 template <class L, bool SCALED = false, class BcBase>
 __device__ __forceinline__ void moving_wall(float (&f)[L::Q], uint32_t nib_solid, const float* bc, uint32_t T,
-                                            BcBase&& bc_base) {
+                                            BcBase&& bc_base, uint32_t warp_any = ~0u) {
     constexpr int Q = L::Q, D = L::D;
     static_for<1, Q>([&](auto qc) {
         constexpr int q = qc.value;
+        if (!((warp_any >> q) & 1u)) return;
         if ((nib_solid >> q) & 1u) {
             const uint64_t b = bc_base(qc);
             float cu = 0.f;
@@ -969,11 +972,12 @@ __device__ __forceinline__ void fused_links(float (&f)[L::Q], const uint2 lt, co
 // its code would raise the register demand of every kernel beyond the budget of 5 CTAs per SM.
 // STAGED: the pull loads read the tile's shared-memory stage `stage` (stage_off; double buffer)
 // instead of global memory.
-template <class L, int METHOD, bool F16C, int COLL, int LES, bool FAST = false, bool LINKS = false,
-          bool STAGED = false>
-__device__ __forceinline__ void tile_step(const StepArgs& a, const uint32_t tile, const uint32_t tid,
-                                          const ClosureDev* cl = nullptr, float4* fbuf = nullptr,
-                                          int32_t near = -1, const void* stage = nullptr) {
+// GENERAL = false is the form of a warp whose cells and pull neighbours are all plain FLUID: no
+// flag is read and the code is straight-line from the loads to the stores; GENERAL = true reads
+// the flags and handles every boundary.
+template <class L, int METHOD, bool F16C, int COLL, int LES, bool FAST, bool LINKS, bool STAGED, bool GENERAL>
+__device__ __forceinline__ void tile_cell(const StepArgs& a, const uint32_t tile, const uint32_t tid,
+                                          const ClosureDev* cl, float4* fbuf, const void* stage) {
     using P = Pop<F16C>;
     using S = typename P::T;
     constexpr int Q = L::Q, D = L::D, K = D + 1;
@@ -1002,14 +1006,9 @@ __device__ __forceinline__ void tile_step(const StepArgs& a, const uint32_t tile
     const uint32_t bz = a.lay.d_nty.div(byz);
     const uint32_t by = byz - bz * (uint32_t)a.lay.nty;
 
-    // ---- are this warp's cells and their pull neighbours all plain FLUID?  (bit w of the tile's
-    // mask byte; the vote makes the value warp-uniform to the compiler: uniform branches below)
-    const uint32_t mask = near >= 0 ? (uint32_t)near : (uint32_t)__ldg(a.tile_near + tile);
-    const bool clean = __all_sync(0xffffffffu, ((mask >> (tid >> 5)) & 1u) == 0u);
-
     uint8_t flag = 0;
     bool active = true;
-    if (!clean) {
+    if constexpr (GENERAL) {
         flag = __ldg(a.flags + n);
         // is_valid_thread (src/lbm/kernels/utils/checks.mojo:55-60); the learned closure keeps
         // every lane for its warp-wide products, the invalid ones write nothing
@@ -1068,7 +1067,7 @@ __device__ __forceinline__ void tile_step(const StepArgs& a, const uint32_t tile
         });
     }
 
-    if (!clean) {
+    if constexpr (GENERAL) {
         // ---- neighbour flags at x - c_q, as masks built when the flags last changed
         // (cell_solid_masks: set_adjacent_flags, ops/load_and_store.mojo:270-291)
         uint32_t raw_solid = 0u, nib_solid = 0u;
@@ -1131,6 +1130,20 @@ __device__ __forceinline__ void tile_step(const StepArgs& a, const uint32_t tile
             st(foA + own + (int32_t)(T * pos), f[neg]);
         });
     }
+}
+
+template <class L, int METHOD, bool F16C, int COLL, int LES, bool FAST = false, bool LINKS = false,
+          bool STAGED = false>
+__device__ __forceinline__ void tile_step(const StepArgs& a, const uint32_t tile, const uint32_t tid,
+                                          const ClosureDev* cl = nullptr, float4* fbuf = nullptr,
+                                          int32_t near = -1, const void* stage = nullptr) {
+    // ---- are this warp's cells and their pull neighbours all plain FLUID?  (bit w of the tile's
+    // mask byte; the vote makes the choice warp-uniform)
+    const uint32_t mask = near >= 0 ? (uint32_t)near : (uint32_t)__ldg(a.tile_near + tile);
+    if (__all_sync(0xffffffffu, ((mask >> (tid >> 5)) & 1u) == 0u))
+        tile_cell<L, METHOD, F16C, COLL, LES, FAST, LINKS, STAGED, false>(a, tile, tid, cl, fbuf, stage);
+    else
+        tile_cell<L, METHOD, F16C, COLL, LES, FAST, LINKS, STAGED, true>(a, tile, tid, cl, fbuf, stage);
 }
 
 #ifndef LBM_TILE_MIN_BLOCKS
