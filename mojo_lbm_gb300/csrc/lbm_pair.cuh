@@ -268,8 +268,13 @@ __device__ __forceinline__ void pair_step(const StepArgs& a, const uint32_t tile
 
 // Resident CTAs (of 128 threads) per SM the pair kernels are built for: the populations of two
 // cells stay in registers across both collisions, so the budget is wider than the per-cell
-// kernel's.  Float16C and float32 7 (72 registers; measured against 6, 8 and 10 on the Float16C
-// cavity), TRT 6 (80), KBC and D3Q27 4 (128): the SRT kernels run without spilling.
+// kernel's.  Float16C in the fast arithmetic 8 (64 registers: 63.7 GLUPs on the 256^3 Float16C
+// cavity against 61.2 at 7 and 58.0 at 6), float32 and the exact Float16C build 7 (72 registers;
+// at 64 the exact build spills), TRT 6 (80), KBC and D3Q27 4 (128): the SRT kernels run without
+// spilling.
+#ifndef LBM_PAIR_MIN_BLOCKS_F16C_FAST
+#define LBM_PAIR_MIN_BLOCKS_F16C_FAST 8
+#endif
 #ifndef LBM_PAIR_MIN_BLOCKS_F16C
 #define LBM_PAIR_MIN_BLOCKS_F16C 7
 #endif
@@ -279,16 +284,17 @@ __device__ __forceinline__ void pair_step(const StepArgs& a, const uint32_t tile
 #ifndef LBM_PAIR_MIN_BLOCKS_HEAVY
 #define LBM_PAIR_MIN_BLOCKS_HEAVY 4
 #endif
-template <class L, bool F16C, int COLL>
+template <class L, bool F16C, int COLL, bool FAST>
 constexpr int pair_min_blocks() {
     return (COLL == LBM_KBC || L::Q == 27) ? LBM_PAIR_MIN_BLOCKS_HEAVY
            : COLL == LBM_TRT               ? 6
+           : (F16C && FAST)                ? LBM_PAIR_MIN_BLOCKS_F16C_FAST
            : F16C                          ? LBM_PAIR_MIN_BLOCKS_F16C
                                            : LBM_PAIR_MIN_BLOCKS;
 }
 
 template <class L, bool F16C, int COLL, int LES, bool FAST>
-__global__ void __launch_bounds__(kPairThreads, (pair_min_blocks<L, F16C, COLL>())) step_kernel_pair(const StepArgs a) {
+__global__ void __launch_bounds__(kPairThreads, (pair_min_blocks<L, F16C, COLL, FAST>())) step_kernel_pair(const StepArgs a) {
     static_assert(LES != kLesLearned, "the learned closure runs in step_kernel_learned");
     pair_step<L, F16C, COLL, LES, FAST>(a, blockIdx.x, threadIdx.x);
 }
