@@ -264,12 +264,17 @@ __device__ __forceinline__ void collide(float (&f)[L::Q], float tau, const StepA
     }
     if (ddf) rho += 1.f;
     float u[3] = {0.f, 0.f, 0.f};
+    [[maybe_unused]] float ir = 0.f;  // learned closure: 1 / rho
     // A cell with zero momentum (a fluid at rest) takes the signed zeros the divisions would give
     // (rho finite and not zero) without dividing: a zero numerator sends the IEEE division to its
-    // special-case path, a third of its usual rate on this GPU.
-    bool at_rest = fabsf(rho) < __int_as_float(0x7f800000) && rho != 0.f;
+    // special-case path, a third of its usual rate on this GPU.  The learned-closure kernels (held
+    // to a tolerance) multiply by one reciprocal of rho instead.
+    bool at_rest = LES != kLesLearned && fabsf(rho) < __int_as_float(0x7f800000) && rho != 0.f;
     static_for<0, D>([&](auto dc) { at_rest = at_rest && mom[dc.value] == 0.f; });
-    if (at_rest) {
+    if constexpr (LES == kLesLearned) {
+        ir = 1.f / rho;
+        static_for<0, D>([&](auto dc) { u[dc.value] = mom[dc.value] * ir; });
+    } else if (at_rest) {
         static_for<0, D>([&](auto dc) {
             u[dc.value] = __uint_as_float((__float_as_uint(mom[dc.value]) ^ __float_as_uint(rho)) & 0x80000000u);
         });
@@ -309,7 +314,7 @@ __device__ __forceinline__ void collide(float (&f)[L::Q], float tau, const StepA
             const float rho_cs2 = (ddf ? rho - 1.f : rho) * (float)(1.0 / 3.0);
             static_for<0, L::NS>([&](auto nc) {
                 constexpr int n = nc.value, A = sa<L>(n), B = sb<L>(n);
-                P[n] = __fmaf_rn(-rho * u[A], u[B], P[n]);
+                P[n] = __fmaf_rn(-mom[A], u[B], P[n]);  // rho u_a = the momentum
                 if constexpr (A == B) P[n] -= rho_cs2;
             });
         }
@@ -329,7 +334,9 @@ __device__ __forceinline__ void collide(float (&f)[L::Q], float tau, const StepA
         if constexpr (LES) {
             // get_strain_rate_tensor / _norm_squared (moment.mojo:154-215),
             // get_Smagorinsky_LES_tau (src/lbm/kernels/ops/turbulence.mojo:12-38)
-            const float k = -1.f / (2.f * rho * (float)(1.0 / 3.0) * tau_local);
+            // k = -1 / (2 rho cs^2 tau); the learned closure's from 1/rho and the host's 1/tau
+            const float k = LES == kLesLearned ? (-1.5f * a.inv_tau) * ir
+                                               : -1.f / (2.f * rho * (float)(1.0 / 3.0) * tau_local);
             float s2 = 0.f;
             float S[L::NS];
             static_for<0, L::NS>([&](auto nc) {
