@@ -241,11 +241,17 @@ __device__ __forceinline__ void collide_fast(float (&f)[L::Q], const StepArgs& a
         // KBC (KBC_.mojo:180-238), gamma not clamped: beta = 1 / (2 tau_l),
         // dh = f - f_eq - ds, gamma = 2 tau_l - (2 - 2 tau_l) <ds, dh> / (<dh, dh> + 1e-32),
         // <x, y> = sum x y / f_eq (unshifted); f' = f - beta (2 ds + gamma dh)
+        //       = f_eq + (1 - 2 beta) ds + (1 - beta gamma) dh.
+        // One pass over the directions computes f_eq and ds once: dh goes to this thread's
+        // lane-fastest slots of shared memory, f_eq + (1 - 2 beta) ds stays in f; once gamma is
+        // known the update adds (1 - beta gamma) dh.
+        __shared__ float dh_keep[Q][256];
+        const uint32_t slot = threadIdx.x;
         const float beta = 0.5f * rcp_approx(tau_l);
         const float inv_beta = 2.f * tau_l;
+        const float cds = __fmaf_rn(-2.f, beta, 1.f);
         const float a0u = rho * __fmaf_rn(-1.5f, uu, 1.f);  // unshifted: rho (1 - 1.5 uu)
         float sp1 = 0.f, sp2 = 0.f;
-        // pass 1: dh in place of f (f = dh + f_eq + ds is what pass 2 needs)
         auto visit = [&](auto qc, float fe0) {
             constexpr int q = decltype(qc)::value;
             constexpr float w = wf<L>(q);
@@ -255,7 +261,8 @@ __device__ __forceinline__ void collide_fast(float (&f)[L::Q], const StepArgs& a
             const float t = dh * rcp_approx(fe0);
             sp1 = __fmaf_rn(ds, t, sp1);
             sp2 = __fmaf_rn(dh, t, sp2);
-            f[q] = dh;
+            dh_keep[q][slot] = dh;
+            f[q] = __fmaf_rn(cds, ds, fe);
         };
         visit(std::integral_constant<int, 0>{}, wf<L>(0) * a0u);
         static_for<0, NP>([&](auto pc) {
@@ -266,22 +273,8 @@ __device__ __forceinline__ void collide_fast(float (&f)[L::Q], const StepArgs& a
             visit(std::integral_constant<int, q + 1>{}, m);
         });
         const float gamma = inv_beta - ((2.f - inv_beta) * sp1) * rcp_approx(sp2 + 1e-32f);
-        // pass 2: f' = f_eq + (1 - 2 beta) ds + (1 - beta gamma) dh
-        const float cdh = __fmaf_rn(-beta, gamma, 1.f), cds = __fmaf_rn(-2.f, beta, 1.f);
-        const float a0s = __fmaf_rn(rho, __fmaf_rn(-1.5f, uu, 1.f), -ddf);  // shifted
-        auto update = [&](auto qc, float fe) {
-            constexpr int q = decltype(qc)::value;
-            const float ds = kbc_shear<L, q>(P);
-            f[q] = __fmaf_rn(cdh, f[q], __fmaf_rn(cds, ds, fe));
-        };
-        update(std::integral_constant<int, 0>{}, wf<L>(0) * a0s);
-        static_for<0, NP>([&](auto pc) {
-            constexpr int q = 2 * pc.value + 1;
-            float p, m;
-            feq_pair_fast<L, q>(a0s, rho, u, uc2, p, m);
-            update(std::integral_constant<int, q>{}, p);
-            update(std::integral_constant<int, q + 1>{}, m);
-        });
+        const float cdh = __fmaf_rn(-beta, gamma, 1.f);
+        static_for<0, Q>([&](auto qc) { f[qc.value] = __fmaf_rn(cdh, dh_keep[qc.value][slot], f[qc.value]); });
     }
 }
 
