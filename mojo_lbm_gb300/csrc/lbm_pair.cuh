@@ -127,25 +127,14 @@ __device__ __forceinline__ void pair_cells(const StepArgs& a, const uint32_t til
 
     uint8_t flagA = 0, flagB = 0;
     bool actA = true, actB = true;
-    // cell-solid masks of both cells (written for every cell of a flagged box): x, z the SOLID pull
-    // neighbours of A, B; y, w those with a moving-wall bc
-    uint4 m = make_uint4(0u, 0u, 0u, 0u);
     if (flagged) {
         flagA = __ldg(a.flags + nA);
         flagB = __ldg(a.flags + nA + 1u);
         // is_valid_thread (src/lbm/kernels/utils/checks.mojo:55-60), per cell
         actA = !((flagA & 0x0F) == LBM_FLAG_SOLID || (flagA & LBM_FLAG_EXCLUDE));
         actB = !((flagB & 0x0F) == LBM_FLAG_SOLID || (flagB & LBM_FLAG_EXCLUDE));
-        m = __ldg(reinterpret_cast<const uint4*>(a.cell_masks + nA));
+        if (!actA && !actB) return;
     }
-    // The directions that any cell of the warp bounces back or takes a moving wall in (all 32 lanes
-    // are converged here): a direction no lane needs is skipped by the whole warp.
-    uint32_t bb_any = 0u, mw_any = 0u;
-    if constexpr (GENERAL) {
-        bb_any = __reduce_or_sync(0xffffffffu, m.x | m.z);
-        mw_any = __reduce_or_sync(0xffffffffu, m.y | m.w);
-    }
-    if (flagged && !actA && !actB) return;
 
     const uint32_t lxA = tA & a.mx, ly = (tA >> a.shx) & a.my, lz = tA >> a.shxy;
     const int32_t TQ = (int32_t)(T * Q);
@@ -175,33 +164,35 @@ __device__ __forceinline__ void pair_cells(const StepArgs& a, const uint32_t til
         }
     });
 
-    if (bb_any) {
-        // ---- mid-grid bounce-back on a raw SOLID compare (ops/load_and_store.mojo:216)
-        static_for<1, Q>([&](auto qc) {
-            constexpr int q = qc.value;
-            if ((bb_any >> q) & 1u) {
-                if ((m.x >> q) & 1u) fa[q] = ld(fin + own + (int32_t)(T * opp<L>(q)));
-                if ((m.z >> q) & 1u) fb[q] = ld(fin + own + 1 + (int32_t)(T * opp<L>(q)));
-            }
-        });
-    }
     if (flagged) {
-        if (a.moving && mw_any) {
+        // ---- cell-solid masks of both cells (written for every cell of a flagged box): x, z the
+        // SOLID pull neighbours of A, B; y, w those with a moving-wall bc.  Loaded after the pulls,
+        // whose latency they share.
+        const uint4 m = __ldg(reinterpret_cast<const uint4*>(a.cell_masks + nA));
+        // mid-grid bounce-back on a raw SOLID compare (ops/load_and_store.mojo:216)
+        if (m.x)
+            static_for<1, Q>([&](auto qc) {
+                constexpr int q = qc.value;
+                if ((m.x >> q) & 1u) fa[q] = ld(fin + own + (int32_t)(T * opp<L>(q)));
+            });
+        if (m.z)
+            static_for<1, Q>([&](auto qc) {
+                constexpr int q = qc.value;
+                if ((m.z >> q) & 1u) fb[q] = ld(fin + own + 1 + (int32_t)(T * opp<L>(q)));
+            });
+        if (a.moving && (m.y | m.w)) {
             // moving_wall_bc with the bc of each cell's SOLID pull neighbours
             auto wall = [&](float (&f)[Q], uint32_t nib, uint32_t tc) {
                 int32_t dc[3][3], dp[3][3];
                 tile_deltas<D>(a, bx, by, bz, tc & a.mx, ly, lz, TQ, dc, dp);
                 const uint32_t n = tc + T * tile;
-                moving_wall<L, SCALED>(
-                    f, nib, a.bc, T,
-                    [&](auto qc) -> uint64_t {
-                        constexpr int q = decltype(qc)::value;
-                        constexpr int sx = -L::c(q, 0), sy = -L::c(q, 1), sz = -L::c(q, 2);
-                        const uint32_t mm = (uint32_t)((int32_t)n + dc[0][sx + 1] + dc[1][sy + 1] + dc[2][sz + 1]);
-                        const uint32_t mt = mm / T;
-                        return (uint64_t)(mm - mt * T) + (uint64_t)T * K * mt;
-                    },
-                    mw_any);
+                moving_wall<L, SCALED>(f, nib, a.bc, T, [&](auto qc) -> uint64_t {
+                    constexpr int q = decltype(qc)::value;
+                    constexpr int sx = -L::c(q, 0), sy = -L::c(q, 1), sz = -L::c(q, 2);
+                    const uint32_t mm = (uint32_t)((int32_t)n + dc[0][sx + 1] + dc[1][sy + 1] + dc[2][sz + 1]);
+                    const uint32_t mt = mm / T;
+                    return (uint64_t)(mm - mt * T) + (uint64_t)T * K * mt;
+                });
             };
             if (m.y) wall(fa, m.y, tA);
             if (m.w) wall(fb, m.w, tA + 1u);

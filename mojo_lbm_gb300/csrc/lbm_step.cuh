@@ -483,15 +483,12 @@ namespace lbm {
 // (enum) node, f_q += 6 w_q rho_w (c_q . u_w) with u_w, rho_w read at the solid node.
 // bc_base(q) returns the element offset of component 0 of the pull neighbour's bc.  SCALED: f holds
 // populations times 2^-112 (the fast build's scaled Float16C codes), and so does the added term.
-// warp_any: a superset of nib_solid that is the same in every lane (the warp's union), so that the
-// warp branches past the directions no lane needs.
 template <class L, bool SCALED = false, class BcBase>
 __device__ __forceinline__ void moving_wall(float (&f)[L::Q], uint32_t nib_solid, const float* bc, uint32_t T,
-                                            BcBase&& bc_base, uint32_t warp_any = ~0u) {
+                                            BcBase&& bc_base) {
     constexpr int Q = L::Q, D = L::D;
     static_for<1, Q>([&](auto qc) {
         constexpr int q = qc.value;
-        if (!((warp_any >> q) & 1u)) return;
         if ((nib_solid >> q) & 1u) {
             const uint64_t b = bc_base(qc);
             float cu = 0.f;
