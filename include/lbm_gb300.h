@@ -156,7 +156,9 @@ lbm_status lbm_set_block_threads(lbm_handle* h, int32_t threads);
  * population buffers are not 8-byte (path 3) or 16-byte (path 4) aligned, or a handle with the
  * learned closure or fused links, runs the block-per-tile kernel (or its variant) instead.  The
  * automatic choice is the cell-pair kernel for double-buffer D2Q9 / D3Q19 configurations other than
- * KBC, the block-per-tile kernel for the other qualifying grids, the generic kernel otherwise.  With LBM_ARITH_EXACT all produce identical populations; the
+ * KBC with at least 2432 tiles (two waves of the pair kernel's CTAs on a 152-SM GPU; below that the
+ * step is latency-bound and the per-cell kernel, with two threads per pair, finishes sooner), the
+ * block-per-tile kernel for the other qualifying grids, the generic kernel otherwise.  With LBM_ARITH_EXACT all produce identical populations; the
  * generic kernel always computes the exact arithmetic. */
 lbm_status lbm_set_kernel_path(lbm_handle* h, int32_t path);
 

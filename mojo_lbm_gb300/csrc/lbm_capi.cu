@@ -212,6 +212,9 @@ StepArgs step_args(const lbm_handle* h, const void* f_in, void* f_out, float* bc
 
 bool use_tile(const lbm_handle* h) { return h->step_tile != nullptr && h->path != 1; }
 
+// Two waves of the cell-pair kernel's CTAs (8 per SM) on the 152 SMs of a GB300.
+constexpr uint32_t kPairAutoMinTiles = 2u * 8u * 152u;
+
 // The staged kernel is chosen (path 4) and can run: no learned closure, no fused links.
 bool use_staged(const lbm_handle* h) {
     return h->path == 4 && h->step_staged != nullptr && !h->closure_on && !h->link_table;
@@ -220,7 +223,9 @@ bool use_staged(const lbm_handle* h) {
 // The cell-pair kernel is chosen (path 3) and can run: no learned closure, no fused links.
 // The automatic choice (path 0) takes it where it measured faster than the per-cell kernel: the
 // double-buffer D2Q9 / D3Q19 configurations other than KBC (whose larger register demand halves the
-// pair kernel's occupancy).
+// pair kernel's occupancy) on grids of at least kPairAutoMinTiles tiles.  On fewer tiles the step
+// is latency-bound, and the per-cell kernel, which gives each pair two threads, finishes sooner
+// (the 256^2 D2Q9 cavity, 256 tiles: 3.2 against 4.3 us a step).
 bool use_pair(const lbm_handle* h) {
     return (h->path == 3 || (h->path == 0 && h->pair_auto)) && h->step_pair != nullptr && !h->closure_on &&
            !h->link_table;
@@ -410,7 +415,8 @@ lbm_status lbm_create(const lbm_config_t* cfg, const lbm_grid_t* grid, lbm_handl
                    : grid->lattice == LBM_D2Q9 ? get_staged_step_d2q9(f16, co, les, fast)
                    : grid->lattice == LBM_D3Q19 ? get_staged_step_d3q19(f16, co, les, fast)
                                                 : get_staged_step_d3q27(f16, co, les, fast);
-    h->pair_auto = h->step_pair != nullptr && co != LBM_KBC && grid->lattice != LBM_D3Q27;
+    h->pair_auto = h->step_pair != nullptr && co != LBM_KBC && grid->lattice != LBM_D3Q27 &&
+                   h->lay.ncells / h->lay.T >= kPairAutoMinTiles;
     h->path = 0;
     h->ntiles = h->lay.ncells / h->lay.T;
     h->mx = (uint32_t)grid->tx - 1u;

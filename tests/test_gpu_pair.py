@@ -125,12 +125,23 @@ def test_pair_misaligned_buffers_fall_back(store):
 
 def test_pair_path_selection():
     s = Solver(make_grid("D3Q19", (16, 16, 8), (8, 8, 4)), LBM_Config())
+    assert s.kernel_path == 2  # 8 tiles: the automatic choice is the per-cell kernel
+    s.set_kernel_path(3)
+    assert s.kernel_path == 3
+    s.close()
+    s = Solver(make_grid("D3Q19", (128, 128, 64), (8, 8, 4)), LBM_Config())
     s.set_kernel_path(3)
     assert s.kernel_path == 3
     s.set_kernel_path(2)
     assert s.kernel_path == 2
     s.set_kernel_path(0)
-    assert s.kernel_path == 3  # the automatic choice for D3Q19 SRT
+    assert s.kernel_path == 3  # the automatic choice for D3Q19 SRT on 4096 tiles
+    s.close()
+    s = Solver(make_grid("D2Q9", (1024, 608, 1), (16, 16, 1)), LBM_Config())
+    assert s.kernel_path == 3  # 2432 tiles, the smallest grid the automatic choice gives cell pairs
+    s.close()
+    s = Solver(make_grid("D2Q9", (1024, 592, 1), (16, 16, 1)), LBM_Config())
+    assert s.kernel_path == 2  # 2368 tiles
     s.close()
     for grid, cfg in ((make_grid("D3Q19", (16, 16, 8), (8, 8, 4)), LBM_Config(LBM_method.ESOTERIC_PULL)),
                       (make_grid("D3Q19", (16, 64, 8), (1, 64, 4)), LBM_Config()),

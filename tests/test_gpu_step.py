@@ -251,7 +251,8 @@ def test_fluid_at_rest(f16, kernel, coll, les):
 
 
 def test_kernel_path_selection():
-    assert Solver(make_grid("D3Q19", (16, 16, 8), (8, 8, 4)), LBM_Config()).kernel_path == 3  # cell pairs
+    assert Solver(make_grid("D3Q19", (128, 128, 64), (8, 8, 4)), LBM_Config()).kernel_path == 3  # cell pairs
+    assert Solver(make_grid("D3Q19", (16, 16, 8), (8, 8, 4)), LBM_Config()).kernel_path == 2  # few tiles
     assert Solver(make_grid("D3Q19", (16, 16, 8), (8, 8, 4)), LBM_Config(collision_op="KBC")).kernel_path == 2
     assert Solver(make_grid("D3Q19", (16, 16, 8), (8, 8, 4)),
                   LBM_Config(LBM_method.ESOTERIC_PULL)).kernel_path == 2
