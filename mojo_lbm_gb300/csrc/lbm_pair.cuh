@@ -287,20 +287,19 @@ constexpr int pair_min_blocks() {
 template <class L, bool F16C, int COLL, int LES, bool FAST>
 __global__ void __launch_bounds__(kPairThreads, (pair_min_blocks<L, F16C, COLL, FAST>())) step_kernel_pair(const StepArgs a) {
     static_assert(LES != kLesLearned, "the learned closure runs in step_kernel_learned");
+    pdl_enter();
     pair_step<L, F16C, COLL, LES, FAST>(a, blockIdx.x, threadIdx.x);
 }
 
 template <class L, int METHOD, bool F16C, int COLL, int LES>
 cudaError_t launch_step_pair(const StepArgs& a, int, cudaStream_t s) {
     static_assert(METHOD == LBM_DOUBLE_BUFFER, "the cell-pair kernel is double-buffer only");
-    step_kernel_pair<L, F16C, COLL, LES, false><<<a.lay.ncells / kTileCells, kPairThreads, 0, s>>>(a);
-    return cudaGetLastError();
+    return launch_pdl(step_kernel_pair<L, F16C, COLL, LES, false>, a.lay.ncells / kTileCells, kPairThreads, s, a);
 }
 template <class L, int METHOD, bool F16C, int COLL, int LES>
 cudaError_t launch_step_pair_fast(const StepArgs& a, int, cudaStream_t s) {
     static_assert(METHOD == LBM_DOUBLE_BUFFER, "the cell-pair kernel is double-buffer only");
-    step_kernel_pair<L, F16C, COLL, LES, true><<<a.lay.ncells / kTileCells, kPairThreads, 0, s>>>(a);
-    return cudaGetLastError();
+    return launch_pdl(step_kernel_pair<L, F16C, COLL, LES, true>, a.lay.ncells / kTileCells, kPairThreads, s, a);
 }
 
 }  // namespace lbm

@@ -1168,10 +1168,37 @@ constexpr int tile_min_blocks() {
     else return (L::Q == 9) ? 5 : (heavy ? LBM_TILE_MIN_BLOCKS_HEAVY : LBM_TILE_MIN_BLOCKS);
 }
 
+// Programmatic dependent launch of the step kernels (launch_pdl): wait until the previous grid in
+// the stream has completed and its writes are visible, then let the next grid (the next step) be
+// scheduled onto the SMs while this one runs, so that its launch latency overlaps this step.  The
+// wait comes before any access to the populations, flags or masks; both instructions are no-ops
+// for a grid launched without the attribute.
+__device__ __forceinline__ void pdl_enter() {
+    asm volatile("griddepcontrol.wait;" ::: "memory");
+    asm volatile("griddepcontrol.launch_dependents;" ::: "memory");
+}
+
+// Launches a step kernel with programmatic stream serialization allowed (see pdl_enter).
+template <class Kernel>
+cudaError_t launch_pdl(Kernel kernel, uint32_t grid, uint32_t block, cudaStream_t s, const StepArgs& a) {
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = dim3(grid);
+    cfg.blockDim = dim3(block);
+    cfg.dynamicSmemBytes = 0;
+    cfg.stream = s;
+    cudaLaunchAttribute attr[1];
+    attr[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+    attr[0].val.programmaticStreamSerializationAllowed = 1;
+    cfg.attrs = attr;
+    cfg.numAttrs = 1;
+    return cudaLaunchKernelEx(&cfg, kernel, a);
+}
+
 template <class L, int METHOD, bool F16C, int COLL, int LES, bool FAST = false, bool LINKS = false>
 __global__ void __launch_bounds__(256, (tile_min_blocks<L, COLL, LINKS>()))
     step_kernel_tile(const StepArgs a) {
     static_assert(LES != kLesLearned, "the learned closure runs in step_kernel_learned");
+    pdl_enter();
     tile_step<L, METHOD, F16C, COLL, LES, FAST, LINKS>(a, blockIdx.x, threadIdx.x);
 }
 
@@ -1218,27 +1245,25 @@ cudaError_t launch_step(const StepArgs& a, int threads, cudaStream_t s) {
 
 template <class L, int METHOD, bool F16C, int COLL, int LES>
 cudaError_t launch_step_tile(const StepArgs& a, int, cudaStream_t s) {
-    step_kernel_tile<L, METHOD, F16C, COLL, LES><<<a.lay.ncells / kTileCells, kTileCells, 0, s>>>(a);
-    return cudaGetLastError();
+    return launch_pdl(step_kernel_tile<L, METHOD, F16C, COLL, LES>, a.lay.ncells / kTileCells, kTileCells, s, a);
 }
 
 // The fast-arithmetic build of the block-per-tile kernel (LBM_ARITH_FAST).
 template <class L, int METHOD, bool F16C, int COLL, int LES>
 cudaError_t launch_step_tile_fast(const StepArgs& a, int, cudaStream_t s) {
-    step_kernel_tile<L, METHOD, F16C, COLL, LES, true><<<a.lay.ncells / kTileCells, kTileCells, 0, s>>>(a);
-    return cudaGetLastError();
+    return launch_pdl(step_kernel_tile<L, METHOD, F16C, COLL, LES, true>, a.lay.ncells / kTileCells, kTileCells, s, a);
 }
 
 // The block-per-tile kernel with fused links (lbm_set_links), exact and fast arithmetic.
 template <class L, int METHOD, bool F16C, int COLL, int LES>
 cudaError_t launch_step_tile_links(const StepArgs& a, int, cudaStream_t s) {
-    step_kernel_tile<L, METHOD, F16C, COLL, LES, false, true><<<a.lay.ncells / kTileCells, kTileCells, 0, s>>>(a);
-    return cudaGetLastError();
+    return launch_pdl(step_kernel_tile<L, METHOD, F16C, COLL, LES, false, true>, a.lay.ncells / kTileCells, kTileCells,
+                      s, a);
 }
 template <class L, int METHOD, bool F16C, int COLL, int LES>
 cudaError_t launch_step_tile_links_fast(const StepArgs& a, int, cudaStream_t s) {
-    step_kernel_tile<L, METHOD, F16C, COLL, LES, true, true><<<a.lay.ncells / kTileCells, kTileCells, 0, s>>>(a);
-    return cudaGetLastError();
+    return launch_pdl(step_kernel_tile<L, METHOD, F16C, COLL, LES, true, true>, a.lay.ncells / kTileCells, kTileCells,
+                      s, a);
 }
 
 template <class L, int METHOD, bool F16C, int COLL, int LES>
