@@ -47,3 +47,16 @@ def test_reference_arm_other_ranks_print_nothing(capsys, monkeypatch):
 def test_warmup_below_three_is_rejected():
     with pytest.raises(SystemExit):
         bench.main(["--impl", "reference", "--steps", "4", "--warmup", "2", "--n", "32"])
+
+
+@pytest.mark.parametrize("workload", sorted(bench.WORKLOADS))
+def test_every_workload_has_a_profile_with_its_traffic(workload):
+    """Each benchmark workload's roofline.traffic comes from its committed ncu summary
+    (profiles/<workload>.txt): the file exists, names the workload's bench command, and holds one
+    positive per-launch DRAM byte count."""
+    traffic, src = bench.profiled_traffic(workload)
+    assert src == f"profiles/{workload}.txt"
+    assert traffic is not None and traffic > 0
+    text = (bench.ROOT / src).read_text()
+    assert f"--workload {workload}" in text or workload == "ldc3d_d3q19_256_fp32"
+    assert "--clock-control none" in text
