@@ -260,7 +260,7 @@ __device__ __forceinline__ void pair_step(const StepArgs& a, const uint32_t tile
 // Resident CTAs (of 128 threads) per SM the pair kernels are built for: the populations of two
 // cells stay in registers across both collisions, so the budget is wider than the per-cell
 // kernel's.  Float16C in the fast arithmetic 8 (64 registers: 63.7 GLUPs on the 256^3 Float16C
-// cavity against 61.2 at 7 and 58.0 at 6), float32 and the exact Float16C build 7 (72 registers;
+// cavity against 60.0 at 9, 61.2 at 7 and 58.0 at 6), float32 and the exact Float16C build 7 (72 registers;
 // at 64 the exact build spills), TRT 6 (80), KBC and D3Q27 4 (128): the SRT kernels run without
 // spilling.
 #ifndef LBM_PAIR_MIN_BLOCKS_F16C_FAST
