@@ -260,9 +260,9 @@ __device__ __forceinline__ void pair_step(const StepArgs& a, const uint32_t tile
 // Resident CTAs (of 128 threads) per SM the pair kernels are built for: the populations of two
 // cells stay in registers across both collisions, so the budget is wider than the per-cell
 // kernel's.  Float16C in the fast arithmetic 8 (64 registers: 63.7 GLUPs on the 256^3 Float16C
-// cavity against 60.0 at 9, 61.2 at 7 and 58.0 at 6), float32 and the exact Float16C build 7 (72 registers;
-// at 64 the exact build spills), TRT 6 (80), KBC and D3Q27 4 (128): the SRT kernels run without
-// spilling.
+// cavity against 60.0 at 9, 61.2 at 7 and 58.0 at 6), float32 8 (64 registers, a few spilled
+// bytes in the wall warps' form only: 43.05 GLUPs on the float32 cavity against 42.46 at 7), the
+// exact Float16C build 7 (72 registers; at 64 it spills), TRT 6 (80), KBC and D3Q27 4 (128).
 #ifndef LBM_PAIR_MIN_BLOCKS_F16C_FAST
 #define LBM_PAIR_MIN_BLOCKS_F16C_FAST 8
 #endif
@@ -270,7 +270,7 @@ __device__ __forceinline__ void pair_step(const StepArgs& a, const uint32_t tile
 #define LBM_PAIR_MIN_BLOCKS_F16C 7
 #endif
 #ifndef LBM_PAIR_MIN_BLOCKS
-#define LBM_PAIR_MIN_BLOCKS 7
+#define LBM_PAIR_MIN_BLOCKS 8
 #endif
 #ifndef LBM_PAIR_MIN_BLOCKS_HEAVY
 #define LBM_PAIR_MIN_BLOCKS_HEAVY 4
